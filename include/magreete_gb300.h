@@ -1,0 +1,181 @@
+/*
+ * magreete_gb300 -- C ABI of the GB300 coupled-dipole engine.
+ *
+ * Every entry point takes DEVICE pointers owned by the caller (torch tensors
+ * in the Python host layer), plain sizes and leading dimensions in elements,
+ * and a cudaStream_t (passed as void*) on which all work is enqueued.  No
+ * entry point allocates device memory: scratch space is a caller-provided
+ * workspace whose size the matching *_workspace_bytes function reports.
+ * Return value: MGT_OK (0) or a negative MGT_ERR_* code for errors found on
+ * the host (bad arguments, CUDA launch errors).  Errors found on the device
+ * (zero pivot, a bounded wait that ran out) are written into the workspace's
+ * status words and read back with mgt_workspace_status().
+ *
+ * Complex data is interleaved (re, im): complex128 = two doubles, complex64 =
+ * two floats, exactly torch's layout.  Matrices are row-major.  The system
+ * index of component a of scatterer i is d*i + a (d = 1, 2 or 3), as in the
+ * reference's G0 reshape (Transmission2D.py:279, Transmission3D.py:267).
+ */
+#ifndef MAGREETE_GB300_H
+#define MAGREETE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MGT_OK 0
+#define MGT_ERR_ARG (-1)          /* invalid argument (shape, pointer, kind) */
+#define MGT_ERR_CUDA (-2)         /* a CUDA runtime call failed */
+#define MGT_ERR_SINGULAR (-3)     /* exact zero pivot (torch.linalg.solve raises) */
+#define MGT_ERR_TIMEOUT (-4)      /* a bounded device-side wait ran out */
+#define MGT_ERR_WORKSPACE (-5)    /* workspace smaller than required */
+#define MGT_ERR_UNSUPPORTED (-6)  /* size or mode not supported by this build */
+#define MGT_ERR_NOT_CONVERGED (-7)/* iterative refinement missed its tolerance */
+
+/* Green's-function kinds, one per reference solver class */
+#define MGT_2D_VECTOR 0   /* Transmission2D_vector (TE, 2x2 dyadic) */
+#define MGT_2D_SCALAR 1   /* Transmission2D_scalar (TM) */
+#define MGT_3D_VECTOR 2   /* Transmission3D_vector (3x3 dyadic) */
+#define MGT_3D_SCALAR 3   /* Transmission3D_scalar */
+
+/* element types */
+#define MGT_C128 0   /* complex128: 2 x double */
+#define MGT_C64 1    /* complex64: 2 x float */
+#define MGT_CDF 2    /* double-float complex: 4 x float (re_hi, re_lo, im_hi,
+                        im_lo), re = re_hi + re_lo exactly; ~2^-48 relative */
+
+/* what the propagator kernel writes where the reference's G is NaN */
+#define MGT_NAN_KEEP 0    /* NaN (propagate(): rows fixed up by the host) */
+#define MGT_NAN_FILL 1    /* every entry of the block = fill value
+                             (mean_DOS_measurements: S/V or 0) */
+
+int mgt_abi_version(void);
+const char* mgt_status_string(int status);
+
+/*
+ * System matrix M = I - coef * G(r_i - r_j) with diagonal 1 - shift.
+ * Replaces G0_vector(None) / G0(None) + `-alpha*k0*k0*G` + fill_diagonal_(1)
+ * + the self-term eye subtraction inside solve():
+ *   Transmission2D.py:222-228 (TE), :733-739 (TM),
+ *   Transmission3D.py:197-203 (vector), :709-715 (scalar).
+ * points: (N, dim) float64 device array.  coef = k0^2 * alpha.  shift is
+ * k0^2 alpha S/V (0 without self-interaction), already rounded as the
+ * reference rounds it.  Entries are evaluated in FP64 and written, in one
+ * pass, to up to two (dN x dN) outputs of element types dtype1 / dtype2
+ * (MGT_C128, MGT_C64 or MGT_CDF); out2 may be NULL.
+ */
+int mgt_assemble_system(int kind, const double* points, int64_t n_points, double k0,
+                        double coef_re, double coef_im, double shift_re, double shift_im,
+                        void* out1, int64_t ld1, int dtype1, void* out2, int64_t ld2, int dtype2,
+                        void* stream);
+
+/*
+ * Propagator block matrix coef * G(t_m - s_j) between n_targets targets and
+ * n_sources scatterers: the dense G0(points) of G0_vector / G0
+ * (Transmission2D.py:263-280, :777-785; Transmission3D.py:240-268, :751-777)
+ * with `regularize` / `radius` semantics per kind (the 2D TE class compares
+ * k*R with radius, Transmission2D.py:86-89; the others compare R).
+ * nan_policy: MGT_NAN_KEEP or MGT_NAN_FILL (fill = fill_re + i fill_im, not
+ * multiplied by coef).  transpose = 0 writes (d*n_targets x d*n_sources),
+ * transpose = 1 writes its transpose (used as right-hand sides).
+ */
+int mgt_assemble_propagator(int kind, const double* targets, int64_t n_targets,
+                            const double* sources, int64_t n_sources, double k0,
+                            double coef_re, double coef_im, int regularize, double radius,
+                            int nan_policy, double fill_re, double fill_im, int transpose,
+                            void* out_c128, int64_t ld, void* stream);
+
+/*
+ * Blocked right-looking LU with partial pivoting (row interchanges), in
+ * place: the `torch.linalg.solve` -> LAPACK ?gesv factorisation step of
+ * solve() (Transmission2D.py:230, :742; Transmission3D.py:205, :717).
+ * dtype MGT_C128 (the plain FP64 method) or MGT_C64 (the mixed-precision
+ * method, refined afterwards).  perm (n int32, device) receives the row
+ * permutation: row i of P*A is row perm[i] of A.  Pivots are chosen by
+ * |re|+|im| like LAPACK.  A zero pivot is recorded in the workspace status
+ * (info, 1-based column like LAPACK) and the factorisation continues.
+ */
+int mgt_lu_workspace_bytes(int dtype, int64_t n, size_t* bytes);
+int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm,
+                  void* work, size_t work_bytes, void* stream);
+
+/*
+ * Solve A X = B with the factors of mgt_lu_factor (the ?getrs half of
+ * ?gesv): X = U^-1 L^-1 P B for nrhs columns.  B is not modified.
+ */
+int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_t* perm,
+                 const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
+                 void* work, size_t work_bytes, void* stream);
+
+/*
+ * Read back the device status words of a workspace (synchronises `stream`):
+ * out[0] = MGT_OK or a device error (MGT_ERR_TIMEOUT), out[1] = info (first
+ * zero pivot, 1-based; 0 if none).  Also clears them.
+ */
+int mgt_workspace_status(void* work, int32_t out[2], void* stream);
+
+/*
+ * Residual R = B - M X with M (n x n) in MGT_CDF form, X, B, R complex128
+ * (n x nrhs), computed in double-float arithmetic on the FP32 pipes
+ * (products exact via fma, sums compensated).  `work` must hold
+ * mgt_residual_workspace_bytes(n, nrhs) bytes.  Used by iterative
+ * refinement.
+ */
+int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
+int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X, int64_t ldx,
+                 const void* B, int64_t ldb, void* R, int64_t ldr, int64_t nrhs,
+                 void* work, size_t work_bytes, void* stream);
+
+/*
+ * Mixed-precision solve of M X = B: complex64 LU factors of M (from
+ * mgt_lu_factor with MGT_C64), M in MGT_CDF form for the residual,
+ * refinement until ||B - M X||_F / ||B||_F <= tol or max_iter corrections.
+ * X (complex128) receives the solution.  iters / rel_res (host pointers,
+ * may be NULL) receive the number of corrections and the final relative
+ * residual.  Returns MGT_ERR_NOT_CONVERGED if tol was not met.
+ */
+int mgt_refine_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
+int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int64_t ldlu,
+                      const int32_t* perm, int64_t n, const void* B, int64_t ldb,
+                      void* X, int64_t ldx, int64_t nrhs, double tol, int max_iter,
+                      void* work, size_t work_bytes, int* iters, double* rel_res,
+                      void* stream);
+
+/*
+ * Matrix-free propagation to detectors:
+ *   out[m*d + a, r] = coef * sum_{j,b} G_ab(t_m - s_j) Ek[j*d + b, r] + E0[m*d + a, r]
+ * G is recomputed on the fly in FP64 and never stored; the contraction runs
+ * in FP64 (dtype MGT_C128) or double-float on the FP32 pipes (MGT_CDF).
+ * Ek, E0 and out are complex128 in both cases.  Replaces the dense
+ * G0(points) + matmul of propagate() (Transmission2D.py:190, :701;
+ * Transmission3D.py:163, :675) and propagate_ss().  Rows where the
+ * reference's G is NaN come out NaN; the host applies the reference's
+ * row fix-up.  E0 may be NULL (treated as zero).
+ */
+int mgt_propagate_workspace_bytes(int kind, int64_t n_targets, int64_t n_sources, int64_t nrhs,
+                                  size_t* bytes);
+int mgt_propagate(int kind, int dtype, const double* targets, int64_t n_targets,
+                  const double* sources, int64_t n_sources, double k0, double coef_re,
+                  double coef_im, int regularize, double radius, const void* Ek,
+                  int64_t ld_ek, const void* E0, int64_t ld_e0, void* out, int64_t ld_out,
+                  int64_t nrhs, void* work, size_t work_bytes, void* stream);
+
+/*
+ * Column dots for the DOS: out[i] = sum_k A[k, i] * B[k, i] (no conjugate),
+ * complex128, A and B (n x ncols) row-major.  With A = Gm^T and
+ * B = M^-1 Gm^T, sum_i out[i] = sum((Gm^T Gm) * W) of
+ * mean_DOS_measurements (Transmission2D.py:327) and out[i] is the
+ * diag(Gm W Gm^T) entry of LDOS_measurements (Transmission2D.py:379).
+ */
+int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t n,
+                    int64_t ncols, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGREETE_GB300_H */

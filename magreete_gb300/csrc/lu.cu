@@ -1,0 +1,537 @@
+// K2/K3: blocked right-looking complex LU with partial pivoting, and the
+// matching multi-RHS triangular solves.
+//
+// Per panel of NB columns (the ?getrf loop that torch.linalg.solve reaches
+// in solve(), Transmission2D.py:230 / Transmission3D.py:205):
+//   1. lu_panel_kernel: one cooperative launch factors the (m x NB) panel.
+//      Each CTA keeps a contiguous chunk of panel rows in shared memory; per
+//      column it publishes its local pivot candidate (value, row, row
+//      contents) and the owner of the diagonal row publishes that row; one
+//      grid barrier; every CTA then picks the same global pivot (largest
+//      |re|+|im|, lowest row on ties, as LAPACK's i?amax), swaps, scales and
+//      applies the rank-1 update to its own rows.  One barrier per column.
+//   2. lu_swap_trsm_kernel: applies the panel's row interchanges to every
+//      column outside the panel (one gather/scatter of at most 2*NB rows per
+//      column) and solves L11 U12 = A12 for the columns right of the panel.
+//   3. trailing update A22 -= L21 U12 (a complex GEMM, gemm.cu).
+#include <algorithm>
+#include <mutex>
+
+#include "common.cuh"
+#include "gemm.cuh"
+
+namespace mgt {
+
+constexpr int kMaxPanelBlocks = 256;
+constexpr int kPanelThreads = 256;
+constexpr int kPanelMinRows = 64;
+constexpr size_t kPanelSmemBudget = 200 * 1024;
+
+// Workspace layout (byte offsets), identical for both element types.
+struct LuWsLayout {
+  size_t barrier = 0;     // 2 x u32: count, generation
+  size_t status = 8;      // 2 x i32: error, info
+  size_t nslot = 16;      // i32: slots written by the last panel
+  size_t cand_val = 64;   // 2 x kMaxPanelBlocks x double
+  size_t cand_idx;        // 2 x kMaxPanelBlocks x i32
+  size_t slots;           // 2*NBmax x int2 (pos, src)
+  size_t rowc;            // 2 x NBmax x complex128
+  size_t cand_row;        // 2 x kMaxPanelBlocks x NBmax x complex128
+  size_t total;
+  static constexpr int NBmax = 64;
+  LuWsLayout() {
+    cand_idx = cand_val + 2 * kMaxPanelBlocks * sizeof(double);
+    slots = cand_idx + 2 * kMaxPanelBlocks * sizeof(int);
+    rowc = (slots + 2 * NBmax * sizeof(int2) + 255) & ~size_t(255);
+    cand_row = rowc + 2 * NBmax * sizeof(double2);
+    total = cand_row + 2 * (size_t)kMaxPanelBlocks * NBmax * sizeof(double2);
+  }
+};
+
+template <typename V>
+struct PanelWs {
+  GridBarrier bar;
+  int* status;
+  int* nslot;
+  double* cand_val;
+  int* cand_idx;
+  int2* slots;
+  V* rowc;
+  V* cand_row;
+};
+
+template <typename V>
+static PanelWs<V> panel_ws(void* work) {
+  LuWsLayout L;
+  char* b = (char*)work;
+  PanelWs<V> w;
+  w.bar.count = (unsigned*)(b + L.barrier);
+  w.bar.gen = (unsigned*)(b + L.barrier) + 1;
+  w.status = (int*)(b + L.status);
+  w.nslot = (int*)(b + L.nslot);
+  w.cand_val = (double*)(b + L.cand_val);
+  w.cand_idx = (int*)(b + L.cand_idx);
+  w.slots = (int2*)(b + L.slots);
+  w.rowc = (V*)(b + L.rowc);
+  w.cand_row = (V*)(b + L.cand_row);
+  return w;
+}
+
+__device__ __forceinline__ bool better(double v, int i, double bv, int bi) {
+  return v > bv || (v == bv && i >= 0 && (bi < 0 || i < bi));
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kPanelThreads)
+lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int rows_per_cta,
+                int32_t* __restrict__ perm, PanelWs<cplx<T>> ws) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* S = reinterpret_cast<V*>(smem_raw);
+  __shared__ V U[NB];
+  __shared__ V RC[NB];
+  __shared__ double red_val[kPanelThreads / 32];
+  __shared__ int red_idx[kPanelThreads / 32];
+  __shared__ int s_best, s_p, s_wb;
+  __shared__ int s_piv[NB];
+  __shared__ int slot_pos[2 * NB], slot_src[2 * NB];
+  __shared__ int s_nslot;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = kPanelThreads / 32;
+  const int G = gridDim.x, bid = blockIdx.x;
+  const int r0 = bid * rows_per_cta;
+  const int r1 = min(m, r0 + rows_per_cta);
+  const int nr = max(0, r1 - r0);
+
+  for (int idx = tid; idx < nr * NB; idx += kPanelThreads) {
+    int rr = idx / NB, cc = idx - rr * NB;
+    S[idx] = cc < w ? A[(int64_t)(r0 + rr) * lda + cc] : czero<V>();
+  }
+  __syncthreads();
+
+  for (int c = 0; c < w; ++c) {
+    const int buf = c & 1;
+    // ---- 1. local pivot candidate (rows i >= c of this chunk)
+    double best = -1.0;
+    int bidx = -1;
+    for (int i = max(r0, c) + tid; i < r1; i += kPanelThreads) {
+      double v = (double)cabs1(S[(i - r0) * NB + c]);
+      if (v > best) { best = v; bidx = i; }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      double ov = __shfl_down_sync(0xffffffffu, best, off);
+      int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (better(ov, oi, best, bidx)) { best = ov; bidx = oi; }
+    }
+    if (lane == 0) { red_val[warp] = best; red_idx[warp] = bidx; }
+    __syncthreads();
+    if (warp == 0) {
+      best = lane < nwarps ? red_val[lane] : -1.0;
+      bidx = lane < nwarps ? red_idx[lane] : -1;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        double ov = __shfl_down_sync(0xffffffffu, best, off);
+        int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+        if (better(ov, oi, best, bidx)) { best = ov; bidx = oi; }
+      }
+      if (lane == 0) {
+        s_best = bidx;
+        ws.cand_val[buf * kMaxPanelBlocks + bid] = best;
+        ws.cand_idx[buf * kMaxPanelBlocks + bid] = bidx;
+      }
+    }
+    __syncthreads();
+    // ---- publish the candidate row and (owner only) the diagonal row c
+    {
+      const int bi = s_best;
+      V* dst = ws.cand_row + ((size_t)buf * kMaxPanelBlocks + bid) * NB;
+      if (bi >= 0)
+        for (int k = tid; k < w; k += kPanelThreads) dst[k] = S[(bi - r0) * NB + k];
+      if (c >= r0 && c < r1)
+        for (int k = tid; k < w; k += kPanelThreads) ws.rowc[buf * NB + k] = S[(c - r0) * NB + k];
+    }
+    __threadfence();
+    // ---- 2. one grid barrier per column
+    if (G > 1) {
+      if (!grid_sync(ws.bar, ws.status)) return;
+    } else {
+      __syncthreads();
+    }
+    // ---- 3. global pivot: identical choice in every CTA
+    if (warp == 0) {
+      double bv = -1.0;
+      int bi = -1, bb = -1;
+      for (int q = lane; q < G; q += 32) {
+        double v = __ldcg(ws.cand_val + buf * kMaxPanelBlocks + q);
+        int i = __ldcg(ws.cand_idx + buf * kMaxPanelBlocks + q);
+        if (better(v, i, bv, bi)) { bv = v; bi = i; bb = q; }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        double ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        int ob = __shfl_down_sync(0xffffffffu, bb, off);
+        if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; bb = ob; }
+      }
+      if (lane == 0) { s_p = bi; s_wb = bb; }
+    }
+    __syncthreads();
+    // No valid candidate anywhere (the column is all NaN): keep row c in place.
+    const int p = s_p >= 0 ? s_p : c, wb = s_p >= 0 ? s_wb : -1;
+    for (int k = tid; k < NB; k += kPanelThreads) {
+      V rc = k < w ? ldcg(ws.rowc + buf * NB + k) : czero<V>();
+      RC[k] = rc;
+      U[k] = (k < w && wb >= 0) ? ldcg(ws.cand_row + ((size_t)buf * kMaxPanelBlocks + wb) * NB + k) : rc;
+    }
+    __syncthreads();
+    const V piv = U[c];
+    const bool nz = (piv.x != 0 || piv.y != 0);
+    if (nz && p != c) {
+      if (p >= r0 && p < r1)
+        for (int k = tid; k < w; k += kPanelThreads) S[(p - r0) * NB + k] = RC[k];
+      if (c >= r0 && c < r1)
+        for (int k = tid; k < w; k += kPanelThreads) S[(c - r0) * NB + k] = U[k];
+    }
+    if (bid == 0 && tid == 0) {
+      const int pe = nz ? p : c;
+      s_piv[c] = pe;
+      if (pe != c) {
+        int a = perm[j0 + c], b = perm[j0 + pe];
+        perm[j0 + c] = b;
+        perm[j0 + pe] = a;
+      }
+      if (!nz && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
+    }
+    __syncthreads();
+    // ---- 4. scale the column below the diagonal and update the rest of the panel
+    const int ibeg = max(r0, c + 1);
+    if (nz) {
+      const V inv = crecip(piv);
+      for (int i = ibeg + tid; i < r1; i += kPanelThreads) {
+        V* e = &S[(i - r0) * NB + c];
+        *e = cmul(*e, inv);
+      }
+    }
+    __syncthreads();
+    const int rows = r1 - ibeg, cols = w - c - 1;
+    if (rows > 0 && cols > 0) {
+      for (int idx = tid; idx < rows * cols; idx += kPanelThreads) {
+        int ii = idx / cols, kk = idx - ii * cols;
+        int i = ibeg + ii, k = c + 1 + kk;
+        V l = S[(i - r0) * NB + c];
+        cfms(S[(i - r0) * NB + k], l, U[k]);
+      }
+    }
+    __syncthreads();
+  }
+
+  for (int idx = tid; idx < nr * NB; idx += kPanelThreads) {
+    int rr = idx / NB, cc = idx - rr * NB;
+    if (cc < w) A[(int64_t)(r0 + rr) * lda + cc] = S[idx];
+  }
+
+  // Net effect of the panel's interchanges on the rows they touch: after
+  // them, panel row slot_pos[q] holds the row that was at slot_src[q].
+  if (bid == 0 && warp == 0) {
+    for (int s = lane; s < NB; s += 32) { slot_pos[s] = s; slot_src[s] = s; }
+    if (lane == 0) s_nslot = NB;
+    __syncwarp();
+    for (int s = 0; s < w; ++s) {
+      const int pv = s_piv[s];
+      if (pv == s) continue;
+      int slot = -1;
+      if (pv < NB) {
+        slot = pv;
+      } else {
+        const int ns = s_nslot;
+        for (int base = NB; base < ns && slot < 0; base += 32) {
+          int q = base + lane;
+          unsigned hit = __ballot_sync(0xffffffffu, q < ns && slot_pos[q] == pv);
+          if (hit) slot = base + __ffs(hit) - 1;
+        }
+        if (slot < 0) {
+          slot = ns;
+          if (lane == 0) { slot_pos[ns] = pv; slot_src[ns] = pv; s_nslot = ns + 1; }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) { int t = slot_src[s]; slot_src[s] = slot_src[slot]; slot_src[slot] = t; }
+      __syncwarp();
+    }
+    const int ns = s_nslot;
+    for (int q = lane; q < ns; q += 32) ws.slots[q] = make_int2(slot_pos[q], slot_src[q]);
+    if (lane == 0) *ws.nslot = ns;
+  }
+}
+
+constexpr int kSwapCols = 32;
+
+// Row interchanges for the columns outside the panel, then (right of the
+// panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256)
+lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int nleft_blocks,
+                    PanelWs<cplx<T>> ws) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* buf = reinterpret_cast<V*>(smem_raw);   // [2*NB][kSwapCols]
+  V* L = buf + 2 * NB * kSwapCols;            // [NB][NB]
+  const int tid = threadIdx.x;
+  const bool right = blockIdx.x >= nleft_blocks;
+  const int col0 = right ? j0 + w + (blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
+  const int colend = right ? n : j0;
+  const int ncols = min(kSwapCols, colend - col0);
+  const int m = n - j0;
+  const int ns = min(*ws.nslot, 2 * NB);
+  // gather rows slot_src[q] (all slots: the top w rows are needed by the solve)
+  for (int idx = tid; idx < ns * kSwapCols; idx += blockDim.x) {
+    int q = idx / kSwapCols, cc = idx - q * kSwapCols;
+    int2 sl = ws.slots[q];
+    bool inb = sl.x >= 0 && sl.x < m && sl.y >= 0 && sl.y < m;
+    bool need = inb && ((sl.x != sl.y) || (right && sl.x < w));
+    if (cc < ncols && need) buf[q * kSwapCols + cc] = A[(int64_t)(j0 + sl.y) * lda + col0 + cc];
+  }
+  if (right) {
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+      int i = idx / w, k = idx - i * w;
+      L[i * NB + k] = A[(int64_t)(j0 + i) * lda + j0 + k];
+    }
+  }
+  __syncthreads();
+  if (right) {
+    // 8 lanes per column: lane = col_local * 8 + t8, 4 columns per warp
+    const int warp = tid >> 5, lane = tid & 31;
+    const int cc = warp * 4 + (lane >> 3), t8 = lane & 7;
+    if (cc < kSwapCols) {
+      for (int k = 0; k < w - 1; ++k) {
+        __syncwarp();
+        const V xk = buf[k * kSwapCols + cc];
+        for (int i = k + 1 + t8; i < w; i += 8) cfms(buf[i * kSwapCols + cc], L[i * NB + k], xk);
+      }
+    }
+    __syncthreads();
+  }
+  // scatter: moved rows, and (right of the panel) the solved top w rows
+  for (int idx = tid; idx < ns * kSwapCols; idx += blockDim.x) {
+    int q = idx / kSwapCols, cc = idx - q * kSwapCols;
+    int2 sl = ws.slots[q];
+    bool inb = sl.x >= 0 && sl.x < m && sl.y >= 0 && sl.y < m;
+    bool moved = sl.x != sl.y;
+    bool top = right && sl.x < w;
+    if (cc < ncols && inb && (moved || top)) A[(int64_t)(j0 + sl.x) * lda + col0 + cc] = buf[q * kSwapCols + cc];
+  }
+}
+
+__global__ void iota_kernel(int32_t* perm, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) perm[i] = i;
+}
+
+static int num_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  });
+  return sms;
+}
+
+template <typename T, int NB>
+static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s) {
+  using V = cplx<T>;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(lu_panel_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemBudget);
+    cudaFuncSetAttribute(lu_swap_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
+  });
+  PanelWs<V> ws = panel_ws<V>(work);
+  if (cudaMemsetAsync(work, 0, 64, s) != cudaSuccess) return MGT_ERR_CUDA;
+  iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n);
+  const int sms = std::min(num_sms(), kMaxPanelBlocks);
+  for (int j0 = 0; j0 < n; j0 += NB) {
+    const int w = std::min(NB, n - j0), m = n - j0;
+    int G = std::max(1, std::min(sms, (m + kPanelMinRows - 1) / kPanelMinRows));
+    int rpc = (m + G - 1) / G;
+    size_t smem = (size_t)rpc * NB * sizeof(V);
+    if (smem > kPanelSmemBudget) return MGT_ERR_UNSUPPORTED;
+    V* P = A + (int64_t)j0 * lda + j0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
+      return MGT_ERR_CUDA;
+    const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
+    const int nright = (n - j0 - w + kSwapCols - 1) / kSwapCols;
+    if (nleft + nright > 0) {
+      size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
+      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, s>>>(A, lda, n, j0, w, nleft, ws);
+    }
+    const int rem = n - j0 - w;
+    if (rem > 0) {
+      int e = gemm_sub<T>(rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w, lda,
+                          A + (int64_t)(j0 + w) * lda + j0 + w, lda, s);
+      if (e != MGT_OK) return e;
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- solves
+
+constexpr int kTrsmCols = 32;
+
+// In-place solve of a bs x bs triangular block against bs rows of X
+// (all columns): lower unit (forward) or upper non-unit (backward).
+template <typename T, int BS, bool UPPER>
+__global__ void __launch_bounds__(256)
+trsm_block_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int row0, int bs, cplx<T>* __restrict__ X,
+                  int64_t ldx, int nrhs) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* Ts = reinterpret_cast<V*>(smem_raw);   // [BS][BS]
+  V* Xs = Ts + BS * BS;                       // [BS][kTrsmCols]
+  __shared__ V dinv[BS];
+  const int tid = threadIdx.x;
+  const int col0 = blockIdx.x * kTrsmCols;
+  const int ncols = min(kTrsmCols, nrhs - col0);
+  for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
+    int i = idx / bs, k = idx - i * bs;
+    Ts[i * BS + k] = F[(int64_t)(row0 + i) * ldf + row0 + k];
+  }
+  for (int idx = tid; idx < bs * kTrsmCols; idx += blockDim.x) {
+    int i = idx / kTrsmCols, cc = idx - i * kTrsmCols;
+    if (cc < ncols) Xs[i * kTrsmCols + cc] = X[(int64_t)(row0 + i) * ldx + col0 + cc];
+  }
+  __syncthreads();
+  if (UPPER) {
+    for (int i = tid; i < bs; i += blockDim.x) dinv[i] = crecip(Ts[i * BS + i]);
+    __syncthreads();
+  }
+  const int warp = tid >> 5, lane = tid & 31;
+  const int cc = warp * 4 + (lane >> 3), t8 = lane & 7;
+  if (cc < kTrsmCols) {
+    if (!UPPER) {
+      for (int k = 0; k < bs - 1; ++k) {
+        __syncwarp();
+        const V xk = Xs[k * kTrsmCols + cc];
+        for (int i = k + 1 + t8; i < bs; i += 8) cfms(Xs[i * kTrsmCols + cc], Ts[i * BS + k], xk);
+      }
+    } else {
+      for (int k = bs - 1; k >= 0; --k) {
+        __syncwarp();
+        if (t8 == 0) Xs[k * kTrsmCols + cc] = cmul(Xs[k * kTrsmCols + cc], dinv[k]);
+        __syncwarp();
+        const V xk = Xs[k * kTrsmCols + cc];
+        for (int i = t8; i < k; i += 8) cfms(Xs[i * kTrsmCols + cc], Ts[i * BS + k], xk);
+      }
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < bs * kTrsmCols; idx += blockDim.x) {
+    int i = idx / kTrsmCols, c2 = idx - i * kTrsmCols;
+    if (c2 < ncols) X[(int64_t)(row0 + i) * ldx + col0 + c2] = Xs[i * kTrsmCols + c2];
+  }
+}
+
+template <typename V>
+__global__ void permute_rows_kernel(const V* __restrict__ B, int64_t ldb, const int32_t* __restrict__ perm,
+                                    V* __restrict__ X, int64_t ldx, int n, int nrhs) {
+  int i = blockIdx.y;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && c < nrhs) X[(int64_t)i * ldx + c] = B[(int64_t)perm[i] * ldb + c];
+}
+
+template <typename T>
+static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* perm, const cplx<T>* B,
+                         int64_t ldb, cplx<T>* X, int64_t ldx, int nrhs, cudaStream_t s) {
+  using V = cplx<T>;
+  constexpr int BS = 64;
+  static std::once_flag once;
+  const size_t smem = (BS * BS + BS * kTrsmCols) * sizeof(V);
+  std::call_once(once, [smem] {
+    cudaFuncSetAttribute(trsm_block_kernel<T, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(trsm_block_kernel<T, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (n > 65535) return MGT_ERR_UNSUPPORTED;
+  dim3 pg((nrhs + 127) / 128, n);
+  permute_rows_kernel<V><<<pg, 128, 0, s>>>(B, ldb, perm, X, ldx, n, nrhs);
+  const int cblocks = (nrhs + kTrsmCols - 1) / kTrsmCols;
+  for (int r0 = 0; r0 < n; r0 += BS) {
+    int bs = std::min(BS, n - r0);
+    trsm_block_kernel<T, BS, false><<<cblocks, 256, smem, s>>>(LU, lda, r0, bs, X, ldx, nrhs);
+    int rem = n - r0 - bs;
+    if (rem > 0) {
+      int e = gemm_sub<T>(rem, nrhs, bs, LU + (int64_t)(r0 + bs) * lda + r0, lda, X + (int64_t)r0 * ldx, ldx,
+                          X + (int64_t)(r0 + bs) * ldx, ldx, s);
+      if (e != MGT_OK) return e;
+    }
+  }
+  const int nblk = (n + BS - 1) / BS;
+  for (int b = nblk - 1; b >= 0; --b) {
+    int r0 = b * BS, bs = std::min(BS, n - r0);
+    trsm_block_kernel<T, BS, true><<<cblocks, 256, smem, s>>>(LU, lda, r0, bs, X, ldx, nrhs);
+    if (r0 > 0) {
+      int e = gemm_sub<T>(r0, nrhs, bs, LU + r0, lda, X + (int64_t)r0 * ldx, ldx, X, ldx, s);
+      if (e != MGT_OK) return e;
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+}  // namespace mgt
+
+using namespace mgt;
+
+extern "C" int mgt_lu_workspace_bytes(int dtype, int64_t n, size_t* bytes) {
+  if (!bytes || n <= 0 || (dtype != MGT_C128 && dtype != MGT_C64)) return MGT_ERR_ARG;
+  *bytes = LuWsLayout().total;
+  return MGT_OK;
+}
+
+extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, void* work,
+                             size_t work_bytes, void* stream) {
+  if (!A || !perm || !work || n <= 0 || lda < n || n > (1 << 20)) return MGT_ERR_ARG;
+  if (work_bytes < LuWsLayout().total) return MGT_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == MGT_C128) return lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s);
+  if (dtype == MGT_C64) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+  return MGT_ERR_ARG;
+}
+
+extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_t* perm,
+                            const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs, void* work,
+                            size_t work_bytes, void* stream) {
+  (void)work; (void)work_bytes;
+  if (!LU || !perm || !B || !X || n <= 0 || nrhs <= 0 || lda < n || ldb < nrhs || ldx < nrhs) return MGT_ERR_ARG;
+  if (B == X) return MGT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == MGT_C128)
+    return lu_solve_impl<double>((const double2*)LU, (int)n, lda, perm, (const double2*)B, ldb, (double2*)X, ldx, (int)nrhs, s);
+  if (dtype == MGT_C64)
+    return lu_solve_impl<float>((const float2*)LU, (int)n, lda, perm, (const float2*)B, ldb, (float2*)X, ldx, (int)nrhs, s);
+  return MGT_ERR_ARG;
+}
+
+extern "C" int mgt_workspace_status(void* work, int32_t out[2], void* stream) {
+  if (!work || !out) return MGT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  LuWsLayout L;
+  int32_t* st = (int32_t*)((char*)work + L.status);
+  if (cudaMemcpyAsync(out, st, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MGT_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MGT_ERR_CUDA;
+  if (cudaMemsetAsync(st, 0, 2 * sizeof(int32_t), s) != cudaSuccess) return MGT_ERR_CUDA;
+  return MGT_OK;
+}

@@ -1,0 +1,276 @@
+// K4: double-float residual R = B - M X and the mixed-precision refinement
+// driver (complex64 LU + double-float residual -> complex128 accuracy).
+//
+// The reference solves once in complex128 (torch.linalg.solve in solve(),
+// Transmission2D.py:230, Transmission3D.py:205).  Here the factorisation runs
+// in complex64 and classical iterative refinement (Wilkinson; Moler 1967)
+// recovers FP64 accuracy: x += LU^-1 (b - M x), with the residual formed in
+// double-float arithmetic from a double-float copy of M.
+#include <algorithm>
+#include <mutex>
+
+#include "common.cuh"
+#include "df.cuh"
+
+namespace mgt {
+
+constexpr int kResRows = 32;   // rows of R per CTA
+constexpr int kResK = 16;      // K chunk staged in shared memory
+
+// Each thread owns rows {ty, ty+16} and columns {tx + 16 j : j < RT}.
+template <int RT>
+__global__ void __launch_bounds__(256)
+residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __restrict__ Xs, int64_t ldxs,
+                   const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R, int64_t ldr, int n,
+                   int ncols, int col_base) {
+  __shared__ float4 Ms[kResRows][kResK + 1];
+  __shared__ float4 Xsh[kResK][16 * RT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int row0 = blockIdx.x * kResRows;
+  float4 acc[2][RT];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < RT; ++j) acc[i][j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k0 = 0; k0 < n; k0 += kResK) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      int idx = tid + 256 * q;
+      int r = idx >> 4, kk = idx & 15;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row0 + r < n && k0 + kk < n) v = M[(int64_t)(row0 + r) * ldm + k0 + kk];
+      Ms[r][kk] = v;
+    }
+    for (int idx = tid; idx < kResK * 16 * RT; idx += 256) {
+      int kk = idx / (16 * RT), c = idx - kk * (16 * RT);
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k0 + kk < n && c < ncols) v = Xs[(int64_t)(k0 + kk) * ldxs + col_base + c];
+      Xsh[kk][c] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kResK; ++kk) {
+      float4 a0 = Ms[ty][kk], a1 = Ms[ty + 16][kk];
+#pragma unroll
+      for (int j = 0; j < RT; ++j) {
+        float4 x = Xsh[kk][tx + 16 * j];
+        df_cmac(acc[0][j], a0, x);
+        df_cmac(acc[1][j], a1, x);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    int r = row0 + ty + 16 * i;
+    if (r >= n) continue;
+#pragma unroll
+    for (int j = 0; j < RT; ++j) {
+      int c = tx + 16 * j;
+      if (c < ncols) {
+        double2 b = B[(int64_t)r * ldb + col_base + c];
+        double2 mx = df_join(acc[i][j]);
+        R[(int64_t)r * ldr + col_base + c] = make_double2(b.x - mx.x, b.y - mx.y);
+      }
+    }
+  }
+}
+
+__global__ void split_df_kernel(const double2* __restrict__ X, int64_t ldx, float4* __restrict__ Y, int64_t ldy,
+                                int n, int ncols) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * ncols) return;
+  int r = (int)(idx / ncols), c = (int)(idx - (int64_t)r * ncols);
+  Y[(int64_t)r * ldy + c] = df_split(X[(int64_t)r * ldx + c]);
+}
+
+__global__ void c128_to_c64_kernel(const double2* __restrict__ X, int64_t ldx, float2* __restrict__ Y, int64_t ldy,
+                                   int n, int ncols) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * ncols) return;
+  int r = (int)(idx / ncols), c = (int)(idx - (int64_t)r * ncols);
+  double2 v = X[(int64_t)r * ldx + c];
+  Y[(int64_t)r * ldy + c] = make_float2((float)v.x, (float)v.y);
+}
+
+// X (complex128) = Y (complex64) when assign, X += Y otherwise
+__global__ void c64_into_c128_kernel(const float2* __restrict__ Y, int64_t ldy, double2* __restrict__ X, int64_t ldx,
+                                     int n, int ncols, int assign) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * ncols) return;
+  int r = (int)(idx / ncols), c = (int)(idx - (int64_t)r * ncols);
+  float2 y = Y[(int64_t)r * ldy + c];
+  double2* x = X + (int64_t)r * ldx + c;
+  if (assign) *x = make_double2(y.x, y.y);
+  else *x = make_double2(x->x + (double)y.x, x->y + (double)y.y);
+}
+
+// out[slot] += sum |X|^2 (slot 0 or 1); FP64 accumulation per thread, then atomics
+__global__ void sumsq_kernel(const double2* __restrict__ X, int64_t ldx, int n, int ncols, double* out) {
+  double s = 0.0;
+  int64_t total = (int64_t)n * ncols;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int r = (int)(idx / ncols), c = (int)(idx - (int64_t)r * ncols);
+    double2 v = X[(int64_t)r * ldx + c];
+    s = fma(v.x, v.x, fma(v.y, v.y, s));
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  __shared__ double red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    atomicAdd(out, t);
+  }
+}
+
+template <int RT>
+static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B,
+                            int64_t ldb, double2* R, int64_t ldr, int n, int ncols, int col_base, cudaStream_t s) {
+  residual_df_kernel<RT><<<(n + kResRows - 1) / kResRows, 256, 0, s>>>(M, ldm, Xs, ldxs, B, ldb, R, ldr, n, ncols,
+                                                                        col_base);
+}
+
+static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb,
+                         double2* R, int64_t ldr, int n, int nrhs, float4* Xs, cudaStream_t s) {
+  int64_t tot = (int64_t)n * nrhs;
+  split_df_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ldx, Xs, nrhs, n, nrhs);
+  for (int c0 = 0; c0 < nrhs; c0 += 128) {
+    int nc = std::min(128, nrhs - c0);
+    int rt = (nc + 15) / 16;
+    switch (rt) {
+      case 1: launch_residual<1>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
+      case 2: launch_residual<2>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
+      case 3: case 4: launch_residual<4>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
+      default: launch_residual<8>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+// refinement workspace layout
+struct RefineWs {
+  float4* Xs;     // n x nrhs double-float copy of X
+  double2* Rr;    // n x nrhs residual
+  float2* R32;    // n x nrhs complex64 residual / right-hand side
+  float2* D32;    // n x nrhs complex64 correction
+  double* norms;  // [0] = ||B||^2, [1] = ||R||^2
+  size_t total;
+  RefineWs(void* base, int64_t n, int64_t r) {
+    char* b = (char*)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = b ? b + off : nullptr; off += (bytes + 255) & ~size_t(255); return p; };
+    Xs = (float4*)take(n * r * sizeof(float4));
+    Rr = (double2*)take(n * r * sizeof(double2));
+    R32 = (float2*)take(n * r * sizeof(float2));
+    D32 = (float2*)take(n * r * sizeof(float2));
+    norms = (double*)take(2 * sizeof(double));
+    total = off;
+  }
+};
+
+}  // namespace mgt
+
+using namespace mgt;
+
+extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_t* perm,
+                            const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs, void* work,
+                            size_t work_bytes, void* stream);
+
+extern "C" int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {
+  if (!bytes || n <= 0 || nrhs <= 0) return MGT_ERR_ARG;
+  *bytes = (size_t)n * nrhs * sizeof(float4) + 256;
+  return MGT_OK;
+}
+
+extern "C" int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X, int64_t ldx, const void* B,
+                            int64_t ldb, void* R, int64_t ldr, int64_t nrhs, void* work, size_t work_bytes,
+                            void* stream) {
+  if (!M || !X || !B || !R || !work || n <= 0 || nrhs <= 0 || ldm < n || ldx < nrhs || ldb < nrhs || ldr < nrhs)
+    return MGT_ERR_ARG;
+  if (n > (1 << 30) || work_bytes < (size_t)n * nrhs * sizeof(float4)) return MGT_ERR_WORKSPACE;
+  return residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, (double2*)R, ldr,
+                       (int)n, (int)nrhs, (float4*)work, (cudaStream_t)stream);
+}
+
+extern "C" int mgt_refine_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {
+  if (!bytes || n <= 0 || nrhs <= 0) return MGT_ERR_ARG;
+  *bytes = RefineWs(nullptr, n, nrhs).total;
+  return MGT_OK;
+}
+
+extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int64_t ldlu, const int32_t* perm,
+                                 int64_t n, const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
+                                 double tol, int max_iter, void* work, size_t work_bytes, int* iters,
+                                 double* rel_res, void* stream) {
+  if (!M || !LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || ldm < n || ldlu < n || ldb < nrhs ||
+      ldx < nrhs || max_iter < 0)
+    return MGT_ERR_ARG;
+  RefineWs w(work, n, nrhs);
+  if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nn = (int)n, nr = (int)nrhs;
+  const int64_t tot = n * nrhs;
+  const unsigned eg = (unsigned)((tot + 255) / 256);
+  const double2* Bd = (const double2*)B;
+  double2* Xd = (double2*)X;
+  double h[2];
+  if (cudaMemsetAsync(w.norms, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
+  sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(Bd, ldb, nn, nr, w.norms);
+  // x0 = LU^-1 b in complex64
+  c128_to_c64_kernel<<<eg, 256, 0, s>>>(Bd, ldb, w.R32, nr, nn, nr);
+  int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
+  if (e != MGT_OK) return e;
+  c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 1);
+  double prev = 0.0, rel = 0.0;
+  int it = 0;
+  for (;; ++it) {
+    e = residual_impl((const float4*)M, ldm, Xd, ldx, Bd, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+    if (e != MGT_OK) return e;
+    if (cudaMemsetAsync(w.norms + 1, 0, sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
+    sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, w.norms + 1);
+    if (cudaMemcpyAsync(h, w.norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MGT_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MGT_ERR_CUDA;
+    rel = h[0] > 0 ? sqrt(h[1] / h[0]) : sqrt(h[1]);
+    if (rel <= tol || it >= max_iter) break;
+    if (it > 0 && !(rel < 0.9 * prev)) break;  // stagnation or divergence
+    prev = rel;
+    c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
+    e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
+    if (e != MGT_OK) return e;
+    c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
+  }
+  if (iters) *iters = it;
+  if (rel_res) *rel_res = rel;
+  if (cudaGetLastError() != cudaSuccess) return MGT_ERR_CUDA;
+  return (rel <= tol && rel == rel) ? MGT_OK : MGT_ERR_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------- DOS dots
+
+__global__ void column_dots_kernel(const double2* __restrict__ A, int64_t lda, const double2* __restrict__ B,
+                                   int64_t ldb, int n, int ncols, int rows_per_block, double2* out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  int r0 = blockIdx.y * rows_per_block, r1 = min(n, r0 + rows_per_block);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int r = r0; r < r1; ++r) cfma(acc, A[(int64_t)r * lda + c], B[(int64_t)r * ldb + c]);
+  atomicAdd(&out[c].x, acc.x);
+  atomicAdd(&out[c].y, acc.y);
+}
+
+extern "C" int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t n, int64_t ncols,
+                               void* out, void* stream) {
+  if (!A || !B || !out || n <= 0 || ncols <= 0 || lda < ncols || ldb < ncols) return MGT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(out, 0, ncols * sizeof(double2), s) != cudaSuccess) return MGT_ERR_CUDA;
+  int rpb = 64;
+  dim3 grid((unsigned)((ncols + 127) / 128), (unsigned)((n + rpb - 1) / rpb));
+  if (grid.y > 65535) { rpb = (int)((n + 65534) / 65535); grid.y = (unsigned)((n + rpb - 1) / rpb); }
+  column_dots_kernel<<<grid, 128, 0, s>>>((const double2*)A, lda, (const double2*)B, ldb, (int)n, (int)ncols, rpb,
+                                          (double2*)out);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}

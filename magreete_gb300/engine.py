@@ -1,0 +1,293 @@
+"""Device-side building blocks over the C ABI (torch tensors as device memory).
+
+Every function here takes and returns CUDA tensors and enqueues work on the
+current torch CUDA stream through ``libmagreete_gb300.so``.  There is no CPU
+path: a missing library or a non-CUDA tensor is an error.
+
+Precision methods
+-----------------
+``"fp64"`` (the plain method, the drop-in default): complex128 assembly,
+complex128 LU with partial pivoting, complex128 triangular solves.
+
+``"mixed"``: one assembly pass writes the matrix in complex64 (for the LU) and
+in double-float form (for residuals); the LU runs in complex64 and iterative
+refinement with double-float residuals brings the solution to a relative
+residual ``tol`` (1e-10 by default), i.e. complex128-level accuracy.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+KIND_CODE = {"2d_vector": L.MGT_2D_VECTOR, "2d_scalar": L.MGT_2D_SCALAR,
+             "3d_vector": L.MGT_3D_VECTOR, "3d_scalar": L.MGT_3D_SCALAR}
+KIND_DIMS = {"2d_vector": (2, 2), "2d_scalar": (2, 1), "3d_vector": (3, 3), "3d_scalar": (3, 1)}
+
+DEFAULT_TOL = 1e-10
+DEFAULT_MAX_ITER = 10
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _need_cuda(t, name):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+
+
+def device_of(*tensors):
+    for t in tensors:
+        if isinstance(t, torch.Tensor) and t.is_cuda:
+            return t.device
+    if not torch.cuda.is_available():
+        raise RuntimeError("magreete_gb300 needs a CUDA GPU; none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def points_to(points, device, dim):
+    p = torch.as_tensor(points)
+    p = p.reshape(-1, dim).to(device=device, dtype=torch.float64).contiguous()
+    return p
+
+
+def workspace(nbytes, device):
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+# ------------------------------------------------------------------ assembly
+
+def assemble_system(kind, points, k0, coef, shift, formats=("c128",)):
+    """M = I - coef * G with diagonal 1 - shift, written in each of
+    ``formats`` ("c128", "c64", "cdf").  Returns a tuple of tensors; "cdf"
+    comes back as a float32 tensor of shape (n, n, 4)."""
+    lib = L.load()
+    _need_cuda(points, "points")
+    dim, d = KIND_DIMS[kind]
+    N = points.shape[0]
+    n = d * N
+    outs, specs = [], []
+    for f in formats:
+        if f == "c128":
+            t = torch.empty((n, n), dtype=torch.complex128, device=points.device)
+            specs.append((t, n, L.MGT_C128))
+        elif f == "c64":
+            t = torch.empty((n, n), dtype=torch.complex64, device=points.device)
+            specs.append((t, n, L.MGT_C64))
+        elif f == "cdf":
+            t = torch.empty((n, n, 4), dtype=torch.float32, device=points.device)
+            specs.append((t, n, L.MGT_CDF))
+        else:
+            raise ValueError(f"unknown format {f}")
+        outs.append(t)
+    if len(specs) > 2:
+        raise ValueError("at most two formats per assembly pass")
+    s2 = specs[1] if len(specs) > 1 else (None, 0, 0)
+    coef = complex(coef)
+    shift = complex(shift)
+    L.check(lib.mgt_assemble_system(KIND_CODE[kind], _ptr(points), N, float(k0), coef.real, coef.imag,
+                                    shift.real, shift.imag, _ptr(specs[0][0]), specs[0][1], specs[0][2],
+                                    _ptr(s2[0]), s2[1], s2[2], _stream()), "mgt_assemble_system")
+    return tuple(outs)
+
+
+def assemble_propagator(kind, targets, sources, k0, coef=1.0, regularize=False, radius=0.0,
+                        nan_fill=None, transpose=False):
+    """Dense coef * G(t - s) (d*T x d*S complex128), or its transpose.
+    nan_fill=None keeps NaN where the reference has NaN; a complex value
+    replaces every entry of such a block."""
+    lib = L.load()
+    _need_cuda(targets, "targets")
+    dim, d = KIND_DIMS[kind]
+    T, S = targets.shape[0], sources.shape[0]
+    shape = (d * S, d * T) if transpose else (d * T, d * S)
+    out = torch.empty(shape, dtype=torch.complex128, device=targets.device)
+    coef = complex(coef)
+    fill = complex(nan_fill) if nan_fill is not None else 0j
+    L.check(lib.mgt_assemble_propagator(KIND_CODE[kind], _ptr(targets), T, _ptr(sources), S, float(k0),
+                                        coef.real, coef.imag, int(bool(regularize)), float(radius),
+                                        L.MGT_NAN_KEEP if nan_fill is None else L.MGT_NAN_FILL,
+                                        fill.real, fill.imag, int(bool(transpose)), _ptr(out), shape[1],
+                                        _stream()), "mgt_assemble_propagator")
+    return out
+
+
+# ------------------------------------------------------------------ LU
+
+class LUFactors:
+    """In-place LU factors with their row permutation and workspace."""
+
+    def __init__(self, lu, perm, work, dtype_code):
+        self.lu, self.perm, self.work, self.dtype_code = lu, perm, work, dtype_code
+
+    @property
+    def n(self):
+        return self.lu.shape[0]
+
+
+def lu_factor(A, check_singular=True):
+    """Factor A (complex128 or complex64, n x n, CUDA) in place."""
+    lib = L.load()
+    _need_cuda(A, "A")
+    n = A.shape[0]
+    code = {torch.complex128: L.MGT_C128, torch.complex64: L.MGT_C64}[A.dtype]
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_lu_workspace_bytes(code, n, ctypes.byref(nb)), "mgt_lu_workspace_bytes")
+    work = workspace(nb.value, A.device)
+    perm = torch.empty(n, dtype=torch.int32, device=A.device)
+    L.check(lib.mgt_lu_factor(code, _ptr(A), n, A.stride(0), _ptr(perm), _ptr(work), work.numel(), _stream()),
+            "mgt_lu_factor")
+    f = LUFactors(A, perm, work, code)
+    if check_singular:
+        status_check(f)
+    return f
+
+
+def status_check(f):
+    lib = L.load()
+    st = (ctypes.c_int32 * 2)()
+    L.check(lib.mgt_workspace_status(_ptr(f.work), st, _stream()), "mgt_workspace_status")
+    if st[0] != 0:
+        raise L.MagreeteError(st[0], "mgt_lu_factor (device)")
+    if st[1] != 0:
+        raise torch.linalg.LinAlgError(
+            f"linalg.solve: The solver failed because the input matrix is singular (zero pivot at column {st[1]}).")
+
+
+def lu_solve(f, B):
+    """X = A^-1 B with LU factors f; B (n x R) of the factors' dtype."""
+    lib = L.load()
+    B = B.contiguous()
+    X = torch.empty_like(B)
+    L.check(lib.mgt_lu_solve(f.dtype_code, _ptr(f.lu), f.n, f.lu.stride(0), _ptr(f.perm), _ptr(B), B.shape[1],
+                             _ptr(X), B.shape[1], B.shape[1], ctypes.c_void_p(0), 0, _stream()), "mgt_lu_solve")
+    return X
+
+
+def solve_refined(Mdf, f, B, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER, require=True):
+    """Refined solve of M X = B (B complex128 n x R) with complex64 factors f
+    and the double-float matrix Mdf.  Returns (X, iterations, rel_residual)."""
+    lib = L.load()
+    n = f.n
+    B = B.contiguous()
+    R = B.shape[1]
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_refine_workspace_bytes(n, R, ctypes.byref(nb)), "mgt_refine_workspace_bytes")
+    work = workspace(nb.value, B.device)
+    X = torch.empty_like(B)
+    it = ctypes.c_int(0)
+    rr = ctypes.c_double(0.0)
+    st = lib.mgt_solve_refined(_ptr(Mdf), n, _ptr(f.lu), f.lu.stride(0), _ptr(f.perm), n, _ptr(B), R, _ptr(X), R,
+                               R, float(tol), int(max_iter), _ptr(work), work.numel(), ctypes.byref(it),
+                               ctypes.byref(rr), _stream())
+    if st == L.MGT_ERR_NOT_CONVERGED and not require:
+        return X, it.value, rr.value
+    L.check(st, f"mgt_solve_refined (iterations {it.value}, relative residual {rr.value:.3e})")
+    return X, it.value, rr.value
+
+
+def residual(Mdf, X, B):
+    lib = L.load()
+    n, R = B.shape
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_residual_workspace_bytes(n, R, ctypes.byref(nb)), "mgt_residual_workspace_bytes")
+    work = workspace(nb.value, B.device)
+    Rr = torch.empty_like(B)
+    X, B = X.contiguous(), B.contiguous()
+    L.check(lib.mgt_residual(_ptr(Mdf), n, n, _ptr(X), R, _ptr(B), R, _ptr(Rr), R, R, _ptr(work), work.numel(),
+                             _stream()), "mgt_residual")
+    return Rr
+
+
+# ------------------------------------------------------------------ system solve
+
+def solve_system(kind, points, k0, coef, shift, E0, precision="fp64", tol=DEFAULT_TOL,
+                 max_iter=DEFAULT_MAX_ITER, stats=None):
+    """Solve (I - coef G) X = E0 with diagonal 1 - shift.  E0: (n, R)
+    complex128 CUDA.  Returns X (n, R) complex128."""
+    if precision == "fp64":
+        (M,) = assemble_system(kind, points, k0, coef, shift, ("c128",))
+        f = lu_factor(M)
+        X = lu_solve(f, E0)
+        if stats is not None:
+            stats.update(method="fp64", iterations=0)
+        return X
+    if precision == "mixed":
+        Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
+        f = lu_factor(M32)
+        X, it, rr = solve_refined(Mdf, f, E0, tol, max_iter)
+        if stats is not None:
+            stats.update(method="mixed", iterations=it, rel_residual=rr)
+        return X
+    raise ValueError(f"unknown precision {precision!r} (expected 'fp64' or 'mixed')")
+
+
+class SystemFactorization:
+    """Factorised system matrix kept resident for several right-hand sides
+    (mean DOS, LDOS, frequency re-queries)."""
+
+    def __init__(self, kind, points, k0, coef, shift, precision="fp64", tol=DEFAULT_TOL,
+                 max_iter=DEFAULT_MAX_ITER):
+        self.precision, self.tol, self.max_iter = precision, tol, max_iter
+        if precision == "fp64":
+            (M,) = assemble_system(kind, points, k0, coef, shift, ("c128",))
+            self.Mdf = None
+            self.f = lu_factor(M)
+        elif precision == "mixed":
+            self.Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
+            self.f = lu_factor(M32)
+        else:
+            raise ValueError(f"unknown precision {precision!r}")
+        self.last_iterations = 0
+        self.last_residual = None
+
+    def solve(self, B):
+        if self.precision == "fp64":
+            return lu_solve(self.f, B.to(torch.complex128))
+        X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter)
+        self.last_iterations, self.last_residual = it, rr
+        return X
+
+
+# ------------------------------------------------------------------ propagate
+
+def propagate(kind, targets, sources, k0, coef, Ek, E0=None, regularize=False, radius=0.0, precision="fp64"):
+    """coef * G(targets, sources) @ Ek + E0, matrix-free.  Ek (d*S, R),
+    E0 (d*T, R) or None.  Returns (d*T, R) complex128."""
+    lib = L.load()
+    dim, d = KIND_DIMS[kind]
+    T, S = targets.shape[0], sources.shape[0]
+    Ek = Ek.reshape(d * S, -1).to(torch.complex128).contiguous()
+    R = Ek.shape[1]
+    if E0 is not None:
+        E0 = E0.reshape(d * T, R).to(torch.complex128).contiguous()
+    out = torch.empty((d * T, R), dtype=torch.complex128, device=targets.device)
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_propagate_workspace_bytes(KIND_CODE[kind], T, S, R, ctypes.byref(nb)),
+            "mgt_propagate_workspace_bytes")
+    work = workspace(nb.value, targets.device)
+    coef = complex(coef)
+    code = L.MGT_C128 if precision == "fp64" else L.MGT_CDF
+    L.check(lib.mgt_propagate(KIND_CODE[kind], code, _ptr(targets), T, _ptr(sources), S, float(k0), coef.real,
+                              coef.imag, int(bool(regularize)), float(radius), _ptr(Ek), R, _ptr(E0), R,
+                              _ptr(out), R, R, _ptr(work), work.numel(), _stream()), "mgt_propagate")
+    return out
+
+
+def column_dots(A, B):
+    """out[i] = sum_k A[k, i] B[k, i] (complex128)."""
+    lib = L.load()
+    A, B = A.contiguous(), B.contiguous()
+    n, c = A.shape
+    out = torch.empty(c, dtype=torch.complex128, device=A.device)
+    L.check(lib.mgt_column_dots(_ptr(A), c, _ptr(B), c, n, c, _ptr(out), _stream()), "mgt_column_dots")
+    return out

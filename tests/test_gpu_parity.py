@@ -1,0 +1,200 @@
+"""GPU parity: the CUDA path against the reference's golden vectors and the FP64 oracle.
+
+Tolerances (relative, Frobenius):
+  * FP64 plain method vs the FP64 oracle (exact Bessel functions): 1e-10.
+  * vs the reference's own outputs: 1e-10 for 3D; for 2D the reference's
+    torch.special Bessel functions are off by up to ~2.4e-6 (relative to
+    the large-x envelope) for 5 <= kR <= 10, so 2D is held to 2e-6.
+  * mixed method (complex64 LU + double-float refinement to a 1e-10
+    residual) vs the FP64 oracle: 1e-8.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL_FP64 = 1e-10
+TOL_MIXED = 1e-8
+TOL_REF = {"2d_vector": 2e-6, "2d_scalar": 2e-6, "3d_vector": 1e-10, "3d_scalar": 1e-10}
+
+
+def load(kind):
+    z = np.load(os.path.join(GOLD, f"golden_{kind}.npz"))
+    return {k: z[k] for k in z.files}
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.detach().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def make(kind, pts, precision="fp64", source="plane"):
+    from magreete_gb300 import Transmission2D_scalar, Transmission2D_vector, Transmission3D_scalar, Transmission3D_vector
+    cls = {"2d_vector": Transmission2D_vector, "2d_scalar": Transmission2D_scalar,
+           "3d_vector": Transmission3D_vector, "3d_scalar": Transmission3D_scalar}[kind]
+    return cls(torch.from_numpy(pts), source=source, precision=precision)
+
+
+def sources(kind, s, g, pts):
+    k0, w = float(g["k0"]), float(g["beam_w"])
+    if kind.startswith("2d"):
+        return s.generate_source(torch.from_numpy(pts), k0, g["thetas"], w)
+    if kind == "3d_vector":
+        return s.generate_source(torch.from_numpy(pts), k0, torch.from_numpy(g["u"]), torch.from_numpy(g["p"]), w)
+    return s.generate_source(torch.from_numpy(pts), k0, torch.from_numpy(g["u"]), w)
+
+
+@pytest.fixture(autouse=True)
+def exact_bessel():
+    O.BESSEL_MODE = "exact"
+    yield
+
+
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_sources_match_reference(kind):
+    g = load(kind)
+    s = make(kind, g["points"])
+    assert rel(sources(kind, s, g, g["points"]), g["E0_scat"]) < 1e-14
+    assert rel(sources(kind, s, g, g["det"]), g["E0_det"]) < 1e-14
+    s.source = "beam"
+    assert rel(sources(kind, s, g, g["points"]), g["E0_scat_beam"]) < 1e-13
+    if kind.startswith("2d"):
+        s.source = "point"
+        assert rel(sources(kind, s, g, g["points"]), g["E0_scat_point"]) < TOL_REF[kind]
+
+
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_green_matrix(kind):
+    g = load(kind)
+    pts = g["points"][:12]
+    s = make(kind, pts)
+    k0 = float(g["k0"])
+    if kind == "2d_scalar":
+        G = s.G0(torch.from_numpy(pts), k0).numpy()
+        off = ~np.eye(12, dtype=bool)
+        ref = O.G0(kind, pts, k0, points=pts)
+        assert rel(G[off], ref[off]) < 1e-13
+        assert rel(G[off], g["G_small"][off]) < TOL_REF[kind]
+    else:
+        G = (s.G0_vector(None, k0) if kind == "2d_vector" else s.G0(None, k0)).numpy()
+        assert rel(G, O.G0(kind, pts, k0)) < 1e-13
+        assert rel(G, g["G_small"]) < TOL_REF[kind]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_solve(kind, precision):
+    g = load(kind)
+    s = make(kind, g["points"], precision)
+    k0, alpha, a = float(g["k0"]), complex(g["alpha"]), float(g["radius"])
+    E0 = torch.from_numpy(g["E0_scat"])
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    for kw, key in [({}, "Ek"), ({"self_interaction": False}, "Ek_no_self"), ({"self_interaction_type": "full"}, "Ek_full")]:
+        Ek = s.solve(k0, alpha, a, E0, **kw)
+        assert Ek.dtype == torch.complex128 and Ek.device.type == "cpu"
+        ref = O.solve(kind, g["points"], k0, alpha, a, g["E0_scat"], kw.get("self_interaction", True),
+                      kw.get("self_interaction_type", "Rayleigh"))
+        assert rel(Ek, ref) < tol, key
+        assert rel(Ek, g[key]) < max(tol, TOL_REF[kind]), key
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_propagate(kind, precision):
+    g = load(kind)
+    s = make(kind, g["points"], precision)
+    k0, alpha, a = float(g["k0"]), complex(g["alpha"]), float(g["radius"])
+    det, Ek, E0d = torch.from_numpy(g["det"]), torch.from_numpy(g["Ek"]), torch.from_numpy(g["E0_det"])
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    E = s.propagate(det, Ek, k0, alpha, E0d)
+    assert not torch.isnan(E).any()
+    assert rel(E, O.propagate(kind, g["points"], g["det"], g["Ek"], k0, alpha, g["E0_det"])) < tol
+    assert rel(E, g["E_det"]) < max(tol, TOL_REF[kind])
+    E = s.propagate(det, Ek, k0, alpha, E0d, regularize=True, radius=a)
+    assert rel(E, O.propagate(kind, g["points"], g["det"], g["Ek"], k0, alpha, g["E0_det"], True, a)) < tol
+    assert rel(E, g["E_det_reg"]) < max(tol, TOL_REF[kind])
+    E = s.propagate_ss(det, k0, alpha, E0d, torch.from_numpy(g["E0_scat"]))
+    assert rel(E, O.propagate_ss(kind, g["points"], g["det"], k0, alpha, g["E0_det"], g["E0_scat"])) < tol
+    assert rel(E, g["E_ss"]) < max(tol, TOL_REF[kind])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_dos(kind, precision):
+    g = load(kind)
+    s = make(kind, g["points"], precision)
+    k0, alpha, a = float(g["k0"]), complex(g["alpha"]), float(g["radius"])
+    tol = TOL_FP64 * 10 if precision == "fp64" else TOL_MIXED
+    for pts_key, kw, key in [("dos_pts", {}, "dos"), ("dos_pts_hit", {}, "dos_hit"),
+                             ("dos_pts", {"regularize": True, "discard_absorption": True}, "dos_reg")]:
+        d = float(s.mean_DOS_measurements(torch.from_numpy(g[pts_key]), k0, alpha, a, **kw))
+        ref = O.mean_dos(kind, g["points"], g[pts_key], k0, alpha, a, **kw)
+        assert abs(d - ref) <= tol * abs(ref), key
+        assert abs(d - float(g[key])) <= max(tol, TOL_REF[kind]) * abs(float(g[key])), key
+    l = s.LDOS_measurements(torch.from_numpy(g["dos_pts"][:8]), k0, alpha, a)
+    assert rel(l, O.ldos(kind, g["points"], g["dos_pts"][:8], k0, alpha, a)) < tol
+    assert rel(l, g["ldos"]) < max(tol, TOL_REF[kind])
+    lb = s.batch_LDOS_measurements([torch.from_numpy(g["dos_pts"][:4]), torch.from_numpy(g["dos_pts"][4:8])],
+                                   k0, alpha, a)
+    assert rel(lb, l) < tol
+
+
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
+@pytest.mark.parametrize("n", [1, 7, 64, 65, 300, 1000, 2500])
+def test_lu_random(n, dtype):
+    from magreete_gb300 import engine as E
+    gen = torch.Generator().manual_seed(n)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen)
+    B = torch.randn(n, 5, dtype=torch.complex128, generator=gen)
+    f = E.lu_factor(A.to(dtype).cuda())
+    X = E.lu_solve(f, B.to(dtype).cuda()).cpu().to(torch.complex128)
+    ref = torch.linalg.solve(A.to(dtype).to(torch.complex128), B.to(dtype).to(torch.complex128))
+    tol = 1e-10 if dtype == torch.complex128 else 2e-3
+    assert rel(X, ref) < tol
+    # P A = L U with the returned permutation
+    LU = f.lu.cpu().to(torch.complex128)
+    Lm = torch.tril(LU, -1) + torch.eye(n, dtype=torch.complex128)
+    U = torch.triu(LU)
+    PA = A.to(dtype).to(torch.complex128)[f.perm.cpu().long()]
+    assert rel(Lm @ U, PA) < (1e-13 if dtype == torch.complex128 else 1e-5)
+
+
+def test_singular_matrix_raises():
+    from magreete_gb300 import engine as E
+    A = torch.randn(80, 80, dtype=torch.complex128)
+    A[:, 17] = 0
+    with pytest.raises(torch.linalg.LinAlgError):
+        E.lu_factor(A.cuda())
+
+
+@pytest.mark.parametrize("kind,N,k", [("2d_vector", 1000, 20.0), ("3d_vector", 700, 6.0)])
+def test_mixed_reaches_tolerance_large(kind, N, k):
+    """Config-sized check: the refined mixed solve meets the 1e-10 residual and
+    agrees with the FP64 GPU solve."""
+    rng = np.random.default_rng(5)
+    dim = 2 if kind.startswith("2d") else 3
+    pts = rng.random((N, dim)) - 0.5
+    V = 0.05 / N
+    a = np.sqrt(V / np.pi) if dim == 2 else np.cbrt(3 * V / (4 * np.pi))
+    alpha = V * (1.6 ** 2 - 1)
+    k0 = 2 * np.pi * k
+    s64, smx = make(kind, pts, "fp64"), make(kind, pts, "mixed")
+    thetas = np.arange(16) / 16 * 2 * np.pi
+    if dim == 2:
+        E0 = s64.generate_source(torch.from_numpy(pts), k0, thetas, 0.2)
+    else:
+        u = torch.from_numpy(np.stack([np.cos(thetas), np.sin(thetas), 0 * thetas], 1))
+        p = torch.zeros_like(u); p[:, 2] = 1
+        E0 = s64.generate_source(torch.from_numpy(pts), k0, u, p, 0.2)
+    X64 = s64.solve(k0, alpha, a, E0)
+    Xmx = smx.solve(k0, alpha, a, E0)
+    assert smx.last_stats["rel_residual"] <= 1e-10
+    assert rel(Xmx, X64) < TOL_MIXED
+    M = O.system_matrix(kind, pts, k0, alpha, a)
+    assert O.relative_residual(M, X64.numpy(), E0.reshape(X64.shape).numpy()) < 1e-12
