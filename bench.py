@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Benchmark: solves/s and p50/p99 latency of the mixed-N coupled-dipole request stream.
+
+Workload (one "step" = one window of the stream): requests arrive as a
+Poisson process (mean 200/s); half are 2D TE (unit disk, phi 0.05) and half
+3D dyadic (unit cube, phi 0.1) problems, N log-uniform in [500, 16000],
+k0 L uniform in [2 pi 5, 2 pi 25], 1-64 incident fields each, 20% re-query an
+earlier geometry at a new frequency.  Each request is solved with the mixed
+method (complex64 LU + double-float refinement to a 1e-10 relative residual)
+and propagated to 360 (2D) / 1024 (3D) detectors.
+
+value: requests/s with inputs resident in HBM (all ranks' requests / max time).
+e2e:   the same windows through the public solver-class API with host
+       (numpy) inputs and host results, copies inside the timed region.
+
+--impl reference times the reference algorithm's CPU implementation (the
+numpy/scipy port in oracle/, the reference itself cannot travel) on a
+bounded, size-capped sample of each window.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+WORKLOAD = ("serving stream: Poisson 200 req/s, 50/50 2D-TE disk / 3D-dyadic cube, N log-uniform [500,16000], "
+            "k0L U[2pi*5, 2pi*25], 1-64 RHS, 20% geometry re-queries at a new k0; mixed method refined to 1e-10; "
+            "detectors 360 ring (2D) / 1024 Fibonacci sphere (3D)")
+METRIC = "solves/s (mixed-N 2D/3D request stream, refined to 1e-10 relative residual)"
+CPU_CAP = {"2d": 1500, "3d": 900}   # size cap of the CPU sample (N)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--requests", type=int, default=8, help="requests per step (window)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for nm, v in zip(names, r[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), float(j["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def windows(steps, warmup, per_step, rank):
+    from magreete_gb300 import workloads as W
+    return [W.serving_stream(per_step, seed=7919 * (s + 1) + 104729 * rank) for s in range(warmup + steps)]
+
+
+# ------------------------------------------------------------------ CPU (reference algorithm)
+
+def cpu_sample(problems, budget):
+    """Run the numpy/scipy port of the reference algorithm on the size-capped
+    requests of `problems` until `budget` seconds are used."""
+    from oracle import oracle as O
+    done, t_used = 0, 0.0
+    for prob in problems:
+        cap = CPU_CAP["2d" if prob.kind.startswith("2d") else "3d"]
+        if prob.N > cap:
+            continue
+        t0 = time.perf_counter()
+        pts, det = prob.points.numpy(), prob.detectors.numpy()
+        if prob.kind.startswith("2d"):
+            E0s = O.source_2d(prob.kind, "plane", pts, prob.k0, prob.thetas, 0.2)
+            E0d = O.source_2d(prob.kind, "plane", det, prob.k0, prob.thetas, 0.2)
+        else:
+            E0s = O.source_3d(prob.kind, "plane", pts, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
+            E0d = O.source_3d(prob.kind, "plane", det, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
+        Ek = O.solve(prob.kind, pts, prob.k0, prob.alpha, prob.radius, E0s)
+        O.propagate(prob.kind, pts, det, Ek, prob.k0, prob.alpha, E0d)
+        t_used += time.perf_counter() - t0
+        done += 1
+        if t_used >= budget:
+            break
+    return done, t_used
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    wins = windows(args.steps, args.warmup, args.requests, 0)
+    budget = max(2.0, args.cpu_budget / max(1, args.steps))
+    for w in wins[:args.warmup]:
+        cpu_sample(w[:1], 1.0)
+    tot_n, tot_t = 0, 0.0
+    for w in wins[args.warmup:]:
+        n, t = cpu_sample(w, budget)
+        tot_n, tot_t = tot_n + n, tot_t + t
+    val = tot_n / tot_t if tot_t > 0 else 0.0
+    cores = os.cpu_count()
+    sample = (f"{tot_n} requests of the stream windows with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D) "
+              f"(larger requests take minutes each on CPU and are skipped, so this overstates CPU throughput); "
+              f"numpy/scipy port of the reference algorithm, complex128, {cores} host threads")
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "requests_per_step": args.requests},
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU
+
+def e2e_window(problems, precision):
+    """Public-API pass: host numpy inputs -> solver classes -> host results."""
+    from magreete_gb300 import Transmission2D_vector, Transmission3D_vector
+    h2d = d2h = 0
+    for prob in problems:
+        pts, det = prob.points.numpy(), prob.detectors.numpy()
+        if prob.kind.startswith("2d"):
+            s = Transmission2D_vector(pts, source="plane", precision=precision)
+            E0s = s.generate_source(pts, prob.k0, prob.thetas, 0.2)
+            E0d = s.generate_source(det, prob.k0, prob.thetas, 0.2)
+        else:
+            s = Transmission3D_vector(pts, source="plane", precision=precision)
+            u, p = prob.u.numpy(), prob.p.numpy()
+            E0s = s.generate_source(pts, prob.k0, u, p, 0.2)
+            E0d = s.generate_source(det, prob.k0, u, p, 0.2)
+        Ek = s.solve(prob.k0, prob.alpha, prob.radius, E0s)
+        Ed = s.propagate(det, Ek, prob.k0, prob.alpha, E0d)
+        h2d += 2 * pts.nbytes + 2 * det.nbytes + E0s.numel() * 16 + Ek.numel() * 16 + E0d.numel() * 16
+        d2h += E0s.numel() * 16 + E0d.numel() * 16 + Ek.numel() * 16 + Ed.numel() * 16
+    return h2d, d2h
+
+
+def run_ours(args, rank, world, local):
+    import magreete_gb300  # noqa: F401
+    from magreete_gb300 import _lib
+    from magreete_gb300 import serve
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    _lib.load()
+    wins = windows(args.steps, args.warmup, args.requests, rank)
+    dev_inputs = [[(p.points.to(dev), p.detectors.to(dev)) for p in w] for w in wins]
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for w, di in zip(wins[:args.warmup], dev_inputs[:args.warmup]):
+        serve.serve_sequential(w, args.precision, di)
+    torch.cuda.synchronize()
+    # ---- timed region: device-resident inputs
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    _lib.diag_reset(enable_timing=True)
+    clocks.start()
+    t0 = time.perf_counter()
+    lat, iters, rres = [], [], []
+    for w, di in zip(wins[args.warmup:], dev_inputs[args.warmup:]):
+        res = serve.serve_sequential(w, args.precision, di)
+        lat += [r.latency for r in res]
+        iters += [r.iterations for r in res]
+        rres += [r.rel_residual for r in res]
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches, dom_n, dom_ms, dom_flops, dom_bytes = _lib.diag_read()
+    _lib.diag_reset(enable_timing=False)
+    barrier()
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t)
+    n_req = args.steps * args.requests * world
+    value = n_req / elapsed
+    # ---- e2e through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        barrier()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        h2d = d2h = 0
+        for w in wins[args.warmup:]:
+            a, b = e2e_window(w, args.precision)
+            h2d, d2h = h2d + a, d2h + b
+        torch.cuda.synchronize()
+        e_el = time.perf_counter() - t1
+        if world > 1:
+            t = torch.tensor([e_el], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e_el = float(t)
+        e2e = {"value": n_req / e_el, "unit": "solves/s", "h2d_bytes_per_step": h2d // args.steps,
+               "d2h_bytes_per_step": d2h // args.steps}
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    hbm, bf16, src = measured_peaks()
+    achieved = (dom_flops / (dom_ms * 1e-3) / 1e12) if dom_ms > 0 else None
+    roofline = {"kernel": "cgemm_sub_kernel<float> (LU trailing update, SIMT FP32)", "bound": "tensor",
+                "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                "frac": (achieved / bf16) if achieved else None, "traffic": None,
+                "peak_source": f"bf16_tflops of {src} peaks", "launches": dom_n,
+                "avg_launch_ms": dom_ms / dom_n if dom_n else None,
+                "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None}
+    cpu = None
+    if world == 1:
+        n, t = cpu_sample(wins[args.warmup], args.cpu_budget)
+        cpu = {"value": n / t if t > 0 else 0.0, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} requests of one stream window with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D); "
+                         "numpy/scipy port of the reference algorithm (complex128), all host threads; larger "
+                         "requests skipped, so this overstates CPU throughput"}
+    lat_ms = sorted(1e3 * x for x in lat)
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex64 LU + double-float residual" if args.precision == "mixed" else "complex128",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "requests_per_step": args.requests, "precision": args.precision,
+                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (matrices 24 n^2 bytes)"},
+            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
+            "refinement": {"max_iterations": max(iters), "max_rel_residual": max(rres)},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

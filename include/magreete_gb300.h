@@ -174,6 +174,18 @@ int mgt_propagate(int kind, int dtype, const double* targets, int64_t n_targets,
 int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t n,
                     int64_t ncols, void* out, void* stream);
 
+/*
+ * Diagnostics (no counterpart in the reference, which has no GPU path):
+ * a counter of this library's kernel launches and optional CUDA-event timing
+ * of every launch of the dominant kernel (the LU trailing update), with its
+ * algorithmic flops and DRAM bytes.  mgt_diag_reset zeroes the counters and
+ * turns the timing on or off; mgt_diag_read synchronises on the recorded
+ * events and returns the totals (any pointer may be NULL).
+ */
+int mgt_diag_reset(int enable_timing);
+int mgt_diag_read(uint64_t* launches, uint64_t* dom_launches, double* dom_ms, double* dom_flops,
+                  double* dom_bytes);
+
 #ifdef __cplusplus
 }
 #endif

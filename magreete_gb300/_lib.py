@@ -52,6 +52,9 @@ SIGNATURES = {
     "mgt_propagate": (_i32, [_i32, _i32, _vp, _i64, _vp, _i64, _f64, _f64, _f64, _i32, _f64, _vp, _i64, _vp, _i64,
                              _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_column_dots": (_i32, [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "mgt_diag_reset": (_i32, [_i32]),
+    "mgt_diag_read": (_i32, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(_f64), ctypes.POINTER(_f64), ctypes.POINTER(_f64)]),
 }
 
 _lock = threading.Lock()
@@ -97,3 +100,16 @@ def check(status, where=""):
     if status != MGT_OK:
         raise MagreeteError(status, where)
     return status
+
+
+def diag_reset(enable_timing=False):
+    check(load().mgt_diag_reset(int(bool(enable_timing))), "mgt_diag_reset")
+
+
+def diag_read():
+    """(launches, dominant-kernel launches, ms, flops, bytes) since the last reset."""
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(load().mgt_diag_read(ctypes.byref(a), ctypes.byref(b), ctypes.byref(ms), ctypes.byref(fl),
+                               ctypes.byref(by)), "mgt_diag_read")
+    return a.value, b.value, ms.value, fl.value, by.value

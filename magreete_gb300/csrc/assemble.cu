@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "green.cuh"
+#include "diag.cuh"
 
 namespace mgt {
 
@@ -134,6 +135,7 @@ static cudaError_t launch_system(const double* pts, int n, double k0, double2 co
                                  OutSpec o1, OutSpec o2, cudaStream_t s) {
   dim3 grid((n + kAsmThreads - 1) / kAsmThreads, (n + kAsmRows - 1) / kAsmRows);
   assemble_system_kernel<KIND><<<grid, kAsmThreads, 0, s>>>(pts, n, k0, coef, diag, o1, o2);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -143,6 +145,7 @@ static cudaError_t launch_prop(const double* t, int nt, const double* src, int n
                                int transpose, double2* out, int64_t ld, cudaStream_t s) {
   int ncol = transpose ? nt : ns, nrow = transpose ? ns : nt;
   dim3 grid((ncol + kAsmThreads - 1) / kAsmThreads, (nrow + kAsmRows - 1) / kAsmRows);
+  count_launch();
   if (transpose)
     assemble_propagator_kernel<KIND, true><<<grid, kAsmThreads, 0, s>>>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, out, ld);
   else

@@ -2,6 +2,7 @@
 // complex64).  64 x 64 output tile per CTA, K staged through shared memory
 // 16 at a time, 4 x 4 complex outputs per thread.
 #include "gemm.cuh"
+#include "diag.cuh"
 
 namespace mgt {
 
@@ -70,6 +71,7 @@ int gemm_sub(int M, int N, int K, const cplx<T>* A, int64_t lda, const cplx<T>* 
   if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
   dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
   if (grid.y > 65535) return MGT_ERR_UNSUPPORTED;
+  count_launch();
   cgemm_sub_kernel<T><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }

@@ -19,13 +19,14 @@
 
 #include "common.cuh"
 #include "gemm.cuh"
+#include "diag.cuh"
 
 namespace mgt {
 
 constexpr int kMaxPanelBlocks = 256;
 constexpr int kPanelThreads = 256;
 constexpr int kPanelMinRows = 64;
-constexpr size_t kPanelSmemBudget = 200 * 1024;
+constexpr size_t kPanelSmemBudget = 220 * 1024;
 
 // Workspace layout (byte offsets), identical for both element types.
 struct LuWsLayout {
@@ -353,6 +354,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   PanelWs<V> ws = panel_ws<V>(work);
   if (cudaMemsetAsync(work, 0, 64, s) != cudaSuccess) return MGT_ERR_CUDA;
   iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n);
+  count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
   for (int j0 = 0; j0 < n; j0 += NB) {
     const int w = std::min(NB, n - j0), m = n - j0;
@@ -373,16 +375,21 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     cfg.numAttrs = 1;
     if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
       return MGT_ERR_CUDA;
+    count_launch();
     const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
     const int nright = (n - j0 - w + kSwapCols - 1) / kSwapCols;
     if (nleft + nright > 0) {
       size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
       lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, s>>>(A, lda, n, j0, w, nleft, ws);
+      count_launch();
     }
     const int rem = n - j0 - w;
     if (rem > 0) {
+      dom_begin(s);
       int e = gemm_sub<T>(rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w, lda,
                           A + (int64_t)(j0 + w) * lda + j0 + w, lda, s);
+      // algorithmic work of A22 -= L21 U12: 8 rem^2 w real flops; C read+written once, A and B read once
+      dom_end(s, 8.0 * rem * (double)rem * w, sizeof(V) * (2.0 * rem * (double)rem + 2.0 * rem * (double)w));
       if (e != MGT_OK) return e;
     }
   }
@@ -468,10 +475,12 @@ static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* p
   if (n > 65535) return MGT_ERR_UNSUPPORTED;
   dim3 pg((nrhs + 127) / 128, n);
   permute_rows_kernel<V><<<pg, 128, 0, s>>>(B, ldb, perm, X, ldx, n, nrhs);
+  count_launch();
   const int cblocks = (nrhs + kTrsmCols - 1) / kTrsmCols;
   for (int r0 = 0; r0 < n; r0 += BS) {
     int bs = std::min(BS, n - r0);
     trsm_block_kernel<T, BS, false><<<cblocks, 256, smem, s>>>(LU, lda, r0, bs, X, ldx, nrhs);
+    count_launch();
     int rem = n - r0 - bs;
     if (rem > 0) {
       int e = gemm_sub<T>(rem, nrhs, bs, LU + (int64_t)(r0 + bs) * lda + r0, lda, X + (int64_t)r0 * ldx, ldx,
@@ -483,6 +492,7 @@ static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* p
   for (int b = nblk - 1; b >= 0; --b) {
     int r0 = b * BS, bs = std::min(BS, n - r0);
     trsm_block_kernel<T, BS, true><<<cblocks, 256, smem, s>>>(LU, lda, r0, bs, X, ldx, nrhs);
+    count_launch();
     if (r0 > 0) {
       int e = gemm_sub<T>(r0, nrhs, bs, LU + r0, lda, X + (int64_t)r0 * ldx, ldx, X, ldx, s);
       if (e != MGT_OK) return e;

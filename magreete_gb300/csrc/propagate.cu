@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "green.cuh"
+#include "diag.cuh"
 
 namespace mgt {
 
@@ -171,6 +172,7 @@ template <int KIND, int RT, bool DF>
 static void launch_partial(dim3 grid, const double* t, int nt, const double* s, int ns, double k0, bool reg,
                            double radius, const double2* Ek, int64_t ld_ek, int ncols, int sps, double2* part,
                            cudaStream_t st) {
+  count_launch();
   propagate_partial_kernel<KIND, RT, DF><<<grid, 256, 0, st>>>(t, nt, s, ns, k0, reg, radius, Ek, ld_ek, ncols, sps,
                                                               part);
 }
@@ -260,6 +262,7 @@ extern "C" int mgt_propagate(int kind, int dtype, const double* targets, int64_t
                                  ld_ek, nc, sps, part, st);
     int64_t nrows = (int64_t)nt * d;
     int64_t tot = nrows * nc;
+    count_launch();
     propagate_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(part, nsplit, nrows, nc, coef,
                                                                           e0 ? e0 + c0 : nullptr, ld_e0, o + c0,
                                                                           ld_out);

@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "df.cuh"
+#include "diag.cuh"
 
 namespace mgt {
 
@@ -130,6 +131,7 @@ __global__ void sumsq_kernel(const double2* __restrict__ X, int64_t ldx, int n, 
 template <int RT>
 static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B,
                             int64_t ldb, double2* R, int64_t ldr, int n, int ncols, int col_base, cudaStream_t s) {
+  count_launch();
   residual_df_kernel<RT><<<(n + kResRows - 1) / kResRows, 256, 0, s>>>(M, ldm, Xs, ldxs, B, ldb, R, ldr, n, ncols,
                                                                         col_base);
 }
@@ -137,6 +139,7 @@ static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int6
 static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb,
                          double2* R, int64_t ldr, int n, int nrhs, float4* Xs, cudaStream_t s) {
   int64_t tot = (int64_t)n * nrhs;
+  count_launch();
   split_df_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ldx, Xs, nrhs, n, nrhs);
   for (int c0 = 0; c0 < nrhs; c0 += 128) {
     int nc = std::min(128, nrhs - c0);
@@ -219,11 +222,14 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   double2* Xd = (double2*)X;
   double h[2];
   if (cudaMemsetAsync(w.norms, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
+  count_launch();
   sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(Bd, ldb, nn, nr, w.norms);
   // x0 = LU^-1 b in complex64
+  count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(Bd, ldb, w.R32, nr, nn, nr);
   int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
   if (e != MGT_OK) return e;
+  count_launch();
   c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 1);
   double prev = 0.0, rel = 0.0;
   int it = 0;
@@ -231,17 +237,20 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
     e = residual_impl((const float4*)M, ldm, Xd, ldx, Bd, ldb, w.Rr, nr, nn, nr, w.Xs, s);
     if (e != MGT_OK) return e;
     if (cudaMemsetAsync(w.norms + 1, 0, sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
-    sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, w.norms + 1);
+    count_launch();
+  sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, w.norms + 1);
     if (cudaMemcpyAsync(h, w.norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MGT_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return MGT_ERR_CUDA;
     rel = h[0] > 0 ? sqrt(h[1] / h[0]) : sqrt(h[1]);
     if (rel <= tol || it >= max_iter) break;
     if (it > 0 && !(rel < 0.9 * prev)) break;  // stagnation or divergence
     prev = rel;
-    c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
+    count_launch();
+  c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
     e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
     if (e != MGT_OK) return e;
-    c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
+    count_launch();
+  c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
   }
   if (iters) *iters = it;
   if (rel_res) *rel_res = rel;
@@ -270,6 +279,7 @@ extern "C" int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_
   int rpb = 64;
   dim3 grid((unsigned)((ncols + 127) / 128), (unsigned)((n + rpb - 1) / rpb));
   if (grid.y > 65535) { rpb = (int)((n + 65534) / 65535); grid.y = (unsigned)((n + rpb - 1) / rpb); }
+  count_launch();
   column_dots_kernel<<<grid, 128, 0, s>>>((const double2*)A, lda, (const double2*)B, ldb, (int)n, (int)ncols, rpb,
                                           (double2*)out);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;

@@ -106,7 +106,9 @@ class CoupledDipoleSolver:
         self._say(f"Calculating Green's function at k0L/2pi = {self._k_label(k0)} ({print_statement})")
         tg = self._r_dev if points is None else self._pts(points)
         G = E.assemble_propagator(self.kind, tg, self._r_dev, k0, 1.0, regularize, radius)
-        if points is None if zero_self is None else zero_self:
+        if zero_self is None:
+            zero_self = points is None
+        if zero_self:
             d = self.d
             idx = torch.arange(self.N, device=self._dev)
             Gv = G.view(self.N, d, self.N, d)
@@ -221,9 +223,11 @@ class CoupledDipoleSolver:
         return val.to(_home_device(measure_points, self.r))
 
     def _ldos_from_dots(self, dots, P, k0, alpha, discard_absorption):
+        """Shapes as the reference: (P, 1) for the vector kinds (reshape(M, d, -1).sum(1),
+        Transmission2D.py:387-388), (P,) for the scalar kinds."""
         a = np.real(alpha) if discard_absorption else alpha
         v = torch.imag(dots * complex(self._DOS_PREF[self.kind](k0, a)))
-        return v.reshape(P, self.d).sum(1) if self.d > 1 else v
+        return v.reshape(P, self.d, -1).sum(1) if self.d > 1 else v
 
     def LDOS_measurements(self, measure_points, k0, alpha, radius, self_interaction=True,
                           self_interaction_type="Rayleigh", regularize=False, discard_absorption=False):
