@@ -104,6 +104,24 @@ int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm,
                   void* work, size_t work_bytes, void* stream);
 
 /*
+ * mgt_lu_factor without a workspace argument; no counterpart in the
+ * reference (whose solve is a single torch.linalg.solve call on the CPU).
+ * For callers that cannot obtain device memory at call time -- a C or
+ * Fortran host binding only this library, with no allocator to ask for the
+ * LU workspace and a policy against cudaMalloc after start-up, or a process
+ * whose device memory is already reserved by its own pool.  The scratch is a
+ * 1 MiB device array inside the library, held on every GPU that loads it
+ * until the process exits; n is limited to 65536 (larger: MGT_ERR_UNSUPPORTED).
+ * All calls share that array: calls whose GPU work overlaps race on it, so
+ * serialise them.  The first call on a device looks up the array's device
+ * address; make it before any stream capture.  info (device, 2 x int32, may
+ * be NULL) receives the status words: [0] device error, [1] first zero pivot
+ * (1-based, 0 if none).  Allocates no device memory.
+ */
+int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, int32_t* info,
+                         void* stream);
+
+/*
  * Solve A X = B with the factors of mgt_lu_factor (the ?getrs half of
  * ?gesv): X = U^-1 L^-1 P B for nrhs columns.  B is not modified.
  */

@@ -545,3 +545,66 @@ extern "C" int mgt_workspace_status(void* work, int32_t out[2], void* stream) {
   if (cudaMemsetAsync(st, 0, 2 * sizeof(int32_t), s) != cudaSuccess) return MGT_ERR_CUDA;
   return MGT_OK;
 }
+
+// ---------------------------------------------------------------- no-allocation LU entry point
+//
+// mgt_lu_factor_static: the same LU as mgt_lu_factor, but its scratch space
+// (panel pivot candidates, pivot-row broadcast buffers, grid-barrier counters
+// and status words) lives in the file-scope device array below instead of a
+// caller-provided workspace.  It exists for callers that cannot obtain device
+// memory at call time: a C or Fortran host that binds only this library (no
+// torch caching allocator or other pool to ask for a workspace) and whose
+// process policy forbids cudaMalloc after start-up, or a process that has
+// already reserved all device memory into its own pool.
+//
+// The array takes kStaticLuScratchBytes (1 MiB) of device memory on every GPU
+// that loads the library, until the process exits.  Every call on a device
+// shares it: the call clears the barrier counters and status words it needs
+// at zero before it starts, and two calls whose GPU work overlaps (different
+// streams, or different host threads) race on it and corrupt each other --
+// serialise them.  The first call on each device looks up the array's device
+// address with cudaGetSymbolAddress (the host-side name of a __device__ array
+// is not a device address); make that first call before any stream capture.
+
+namespace mgt {
+constexpr size_t kStaticLuScratchBytes = size_t(1) << 20;
+constexpr int64_t kStaticLuMaxN = 65536;
+static __device__ __align__(256) unsigned char g_lu_static_scratch[kStaticLuScratchBytes];
+
+static int static_lu_scratch(void** out) {
+  static std::mutex mu;
+  static void* per_device[64] = {};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MGT_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!per_device[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_lu_static_scratch) != cudaSuccess || !p) return MGT_ERR_CUDA;
+    per_device[dev] = p;
+  }
+  *out = per_device[dev];
+  return MGT_OK;
+}
+}  // namespace mgt
+
+extern "C" int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, int32_t* info,
+                                    void* stream) {
+  if (!A || !perm || n <= 0 || lda < n) return MGT_ERR_ARG;
+  if (dtype != MGT_C128 && dtype != MGT_C64) return MGT_ERR_ARG;
+  if (n > kStaticLuMaxN) return MGT_ERR_UNSUPPORTED;
+  if (LuWsLayout().total > kStaticLuScratchBytes) return MGT_ERR_WORKSPACE;
+  void* work = nullptr;
+  int e = static_lu_scratch(&work);
+  if (e != MGT_OK) return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  e = dtype == MGT_C128 ? lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s)
+                        : lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+  if (e != MGT_OK) return e;
+  if (info) {
+    LuWsLayout L;
+    if (cudaMemcpyAsync(info, (char*)work + L.status, 2 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s) !=
+        cudaSuccess)
+      return MGT_ERR_CUDA;
+  }
+  return MGT_OK;
+}
