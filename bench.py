@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--phases", action="store_true",
+                    help="print per-phase device times of the transmission configs instead of the stream bench")
     return ap.parse_args()
 
 
@@ -155,7 +157,9 @@ def cpu_sample(problems, budget):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    wins = windows(args.steps, args.warmup, args.requests, 0)
+    from magreete_gb300 import workloads as W
+    # size-capped requests are rare in a short window: each step samples a longer stretch of the stream
+    wins = [W.serving_stream(128, seed=7919 * (s + 1)) for s in range(args.warmup + args.steps)]
     budget = max(2.0, args.cpu_budget / max(1, args.steps))
     for w in wins[:args.warmup]:
         cpu_sample(w[:1], 1.0)
@@ -165,7 +169,7 @@ def run_reference(args, rank, world):
         tot_n, tot_t = tot_n + n, tot_t + t
     val = tot_n / tot_t if tot_t > 0 else 0.0
     cores = os.cpu_count()
-    sample = (f"{tot_n} requests of the stream windows with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D) "
+    sample = (f"{tot_n} requests of the stream (same generator) with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D) "
               f"(larger requests take minutes each on CPU and are skipped, so this overstates CPU throughput); "
               f"numpy/scipy port of the reference algorithm, complex128, {cores} host threads")
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus,
@@ -280,9 +284,10 @@ def run_ours(args, rank, world, local):
                 "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None}
     cpu = None
     if world == 1:
-        n, t = cpu_sample(wins[args.warmup], args.cpu_budget)
+        from magreete_gb300 import workloads as W
+        n, t = cpu_sample(W.serving_stream(256, seed=99991), args.cpu_budget)
         cpu = {"value": n / t if t > 0 else 0.0, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{n} requests of one stream window with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D); "
+               "sample": f"{n} requests of the stream (same generator) with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D); "
                          "numpy/scipy port of the reference algorithm (complex128), all host threads; larger "
                          "requests skipped, so this overstates CPU throughput"}
     lat_ms = sorted(1e3 * x for x in lat)
@@ -301,9 +306,69 @@ def run_ours(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def run_phases(args):
+    """Per-phase device times (CUDA events) of one request: 2D TE N=1000 (64 RHS, 360 detectors),
+    3D dyadic N=4000 (64 RHS, 1024 detectors) and 3D dyadic N=9000, both methods."""
+    from magreete_gb300 import _lib, engine as E, selfterm, serve
+    from magreete_gb300 import workloads as W
+    _lib.load()
+    dev = torch.device("cuda")
+
+    def ev():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    cases = [("2d_te_N1000", W.cfg1(), ("mixed", "fp64")), ("3d_N4000", W.cfg2(), ("mixed", "fp64")),
+             ("3d_N9000", W.cube_problem(9000, 3, 15.0), ("mixed",))]
+    for label, prob, precs in cases:
+        for prec in precs:
+            for rep in range(2):
+                pts, det = prob.points.to(dev), prob.detectors.to(dev)
+                coef = prob.alpha * prob.k0 ** 2
+                shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+                E0s, E0d = serve.incident_fields(prob, pts, det)
+                n, R = prob.n, prob.nrhs
+                B = E0s.reshape(n, R).contiguous()
+                torch.cuda.synchronize()
+                _lib.diag_reset(enable_timing=True)
+                e0 = ev()
+                if prec == "fp64":
+                    (M,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("c128",))
+                    e1 = ev()
+                    f = E.lu_factor(M, check_singular=False)
+                    e2 = ev()
+                    X = E.lu_solve(f, B)
+                    it, rr = 0, None
+                else:
+                    Mdf, M32 = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf", "c64"))
+                    e1 = ev()
+                    f = E.lu_factor(M32, check_singular=False)
+                    e2 = ev()
+                    X, it, rr = E.solve_refined(Mdf, f, B)
+                e3 = ev()
+                E.propagate(prob.kind, det, pts, prob.k0, coef, X, E0d.reshape(-1, R), precision=prec)
+                e4 = ev()
+                torch.cuda.synchronize()
+                _, dn, dms, dfl, dby = _lib.diag_read()
+                _lib.diag_reset(enable_timing=False)
+                if rep == 0:
+                    continue
+                lu = e1.elapsed_time(e2)
+                print(json.dumps({"case": label, "precision": prec, "n": n, "nrhs": R,
+                                  "assemble_ms": e0.elapsed_time(e1), "lu_ms": lu,
+                                  "lu_tflops": 8 / 3 * n ** 3 / lu / 1e9, "solve_ms": e2.elapsed_time(e3),
+                                  "refine_iterations": it, "rel_residual": rr, "propagate_ms": e3.elapsed_time(e4),
+                                  "trailing_update": {"launches": dn, "ms": dms,
+                                                      "tflops": dfl / dms / 1e9 if dms else None}}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.phases:
+        run_phases(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -130,6 +130,19 @@ int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_
                  void* work, size_t work_bytes, void* stream);
 
 /*
+ * Complex GEMM update C (M x N) -= A (M x K) * B (K x N), row-major: the LU
+ * trailing update A22 -= L21 U12 (inside ?getrf of torch.linalg.solve,
+ * Transmission2D.py:230 / Transmission3D.py:205), exposed on its own.
+ * MGT_C128: FP64 SIMT.  MGT_C64 with use_tensor_cores = 0: FP32 SIMT;
+ * use_tensor_cores = 1: tcgen05 kind::tf32 with hi/lo split operands
+ * (TF32x3, FP32-level accuracy), K <= 64, ldc even; needs
+ * mgt_cgemm_workspace_bytes(max(M, N)) bytes of workspace.
+ */
+int mgt_cgemm_workspace_bytes(int64_t nmax, size_t* bytes);
+int mgt_cgemm_sub(int dtype, int use_tensor_cores, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                  const void* B, int64_t ldb, void* C, int64_t ldc, void* work, size_t work_bytes, void* stream);
+
+/*
  * Read back the device status words of a workspace (synchronises `stream`):
  * out[0] = MGT_OK or a device error (MGT_ERR_TIMEOUT), out[1] = info (first
  * zero pivot, 1-based; 0 if none).  Also clears them.

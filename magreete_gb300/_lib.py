@@ -53,6 +53,8 @@ SIGNATURES = {
     "mgt_propagate": (_i32, [_i32, _i32, _vp, _i64, _vp, _i64, _f64, _f64, _f64, _i32, _f64, _vp, _i64, _vp, _i64,
                              _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_column_dots": (_i32, [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "mgt_cgemm_workspace_bytes": (_i32, [_i64, ctypes.POINTER(_sz)]),
+    "mgt_cgemm_sub": (_i32, [_i32, _i32, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _sz, _vp]),
     "mgt_diag_reset": (_i32, [_i32]),
     "mgt_diag_read": (_i32, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                              ctypes.POINTER(_f64), ctypes.POINTER(_f64), ctypes.POINTER(_f64)]),

@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "gemm.cuh"
+#include "gemm_tc.cuh"
 #include "diag.cuh"
 
 namespace mgt {
@@ -342,8 +343,22 @@ static int num_sms() {
   return sms;
 }
 
+// Trailing update: tensor cores (tcgen05 TF32x3) for complex64 when a plan is
+// given, SIMT otherwise (complex128, or no tensor-core scratch).
+static int trailing_update(const TcPlan* tc, int M, int N, int K, const double2* A, int64_t lda, const double2* B,
+                           int64_t ldb, double2* C, int64_t ldc, int*, cudaStream_t s) {
+  (void)tc;
+  return gemm_sub<double>(M, N, K, A, lda, B, ldb, C, ldc, s);
+}
+static int trailing_update(const TcPlan* tc, int M, int N, int K, const float2* A, int64_t lda, const float2* B,
+                           int64_t ldb, float2* C, int64_t ldc, int* status, cudaStream_t s) {
+  if (tc) return gemm_sub_tc(*tc, M, N, K, A, lda, B, ldb, C, ldc, status, s);
+  return gemm_sub<float>(M, N, K, A, lda, B, ldb, C, ldc, s);
+}
+
 template <typename T, int NB>
-static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s) {
+static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s,
+                          const TcPlan* tc = nullptr) {
   using V = cplx<T>;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -386,8 +401,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int rem = n - j0 - w;
     if (rem > 0) {
       dom_begin(s);
-      int e = gemm_sub<T>(rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w, lda,
-                          A + (int64_t)(j0 + w) * lda + j0 + w, lda, s);
+      int e = trailing_update(tc, rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w,
+                              lda, A + (int64_t)(j0 + w) * lda + j0 + w, lda, ws.status, s);
       // algorithmic work of A22 -= L21 U12: 8 rem^2 w real flops; C read+written once, A and B read once
       dom_end(s, 8.0 * rem * (double)rem * w, sizeof(V) * (2.0 * rem * (double)rem + 2.0 * rem * (double)w));
       if (e != MGT_OK) return e;
@@ -505,9 +520,15 @@ static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* p
 
 using namespace mgt;
 
+// Below this order the complex64 trailing update stays on the SIMT pipes.
+constexpr int64_t kTcMinN = 256;
+
+static size_t tc_region_offset() { return (LuWsLayout().total + 1023) & ~size_t(1023); }
+
 extern "C" int mgt_lu_workspace_bytes(int dtype, int64_t n, size_t* bytes) {
   if (!bytes || n <= 0 || (dtype != MGT_C128 && dtype != MGT_C64)) return MGT_ERR_ARG;
   *bytes = LuWsLayout().total;
+  if (dtype == MGT_C64 && n >= kTcMinN) *bytes = tc_region_offset() + tc_scratch_bytes(n);
   return MGT_OK;
 }
 
@@ -517,7 +538,16 @@ extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t
   if (work_bytes < LuWsLayout().total) return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == MGT_C128) return lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s);
-  if (dtype == MGT_C64) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+  if (dtype == MGT_C64) {
+    // tensor-core trailing update when the workspace holds its split buffers,
+    // the rows are 16-byte aligned (even lda) and the driver exposes TMA maps
+    if (n >= kTcMinN && (lda & 1) == 0 && work_bytes >= tc_region_offset() + tc_scratch_bytes(n) && tc_available()) {
+      TcPlan plan;
+      int e = plan.init((char*)work + tc_region_offset(), n);
+      if (e == MGT_OK) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, &plan);
+    }
+    return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+  }
   return MGT_ERR_ARG;
 }
 

@@ -81,8 +81,11 @@ def assemble_system(kind, points, k0, coef, shift, formats=("c128",)):
             t = torch.empty((n, n), dtype=torch.complex128, device=points.device)
             specs.append((t, n, L.MGT_C128))
         elif f == "c64":
-            t = torch.empty((n, n), dtype=torch.complex64, device=points.device)
-            specs.append((t, n, L.MGT_C64))
+            # rows padded to a multiple of 16 elements (128 B): the tensor-core
+            # LU update needs 16-byte aligned rows
+            ld = (n + 15) // 16 * 16
+            t = torch.empty((n, ld), dtype=torch.complex64, device=points.device)[:, :n]
+            specs.append((t, ld, L.MGT_C64))
         elif f == "cdf":
             t = torch.empty((n, n, 4), dtype=torch.float32, device=points.device)
             specs.append((t, n, L.MGT_CDF))
@@ -281,6 +284,24 @@ def propagate(kind, targets, sources, k0, coef, Ek, E0=None, regularize=False, r
                               coef.imag, int(bool(regularize)), float(radius), _ptr(Ek), R, _ptr(E0), R,
                               _ptr(out), R, R, _ptr(work), work.numel(), _stream()), "mgt_propagate")
     return out
+
+
+def cgemm_sub(C, A, B, tensor_cores=True):
+    """C -= A @ B in place (complex; C, A, B CUDA tensors of one dtype)."""
+    lib = L.load()
+    M, K = A.shape
+    N = B.shape[1]
+    code = {torch.complex128: L.MGT_C128, torch.complex64: L.MGT_C64}[C.dtype]
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_cgemm_workspace_bytes(max(M, N), ctypes.byref(nb)), "mgt_cgemm_workspace_bytes")
+    work = workspace(nb.value, C.device)
+    work[:256].zero_()
+    L.check(lib.mgt_cgemm_sub(code, int(bool(tensor_cores)), M, N, K, _ptr(A), A.stride(0), _ptr(B), B.stride(0),
+                              _ptr(C), C.stride(0), _ptr(work), work.numel(), _stream()), "mgt_cgemm_sub")
+    st = int(work[:4].view(torch.int32)[0].item())
+    if st != 0:
+        raise L.MagreeteError(st, "mgt_cgemm_sub (device)")
+    return C
 
 
 def column_dots(A, B):
