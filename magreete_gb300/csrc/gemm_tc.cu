@@ -40,17 +40,20 @@ namespace mgt {
 namespace tc {
 
 constexpr int BM = 128;            // tile rows (M)
-constexpr int BN = 256;            // tile real columns (N')
+constexpr int BN = 128;            // tile real columns (N') = 64 complex columns
 constexpr int BK = 32;             // fp32 elements per 128-byte swizzle row
 constexpr int KR = 128;            // real K of the split buffers (2 * 64)
 constexpr int KBLOCKS = KR / BK;   // 4
 constexpr int STAGES = 2;
 constexpr uint32_t A_TILE = BM * BK * 4;   // 16 KB
-constexpr uint32_t B_TILE = BN * BK * 4;   // 32 KB
-constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 96 KB
-constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t B_TILE = BN * BK * 4;   // 16 KB
+constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 64 KB
+constexpr int CHUNKS = BN / 32;            // epilogue chunks per tile (32 fp32 columns each)
+constexpr int CSLOTS = 4;                  // C chunk ring
+constexpr uint32_t CHUNK_BYTES = BM * 128; // 16 KB
+constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int THREADS = 256;
-constexpr size_t SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* alignment slack */ + 256 /* barriers */;
+constexpr size_t SMEM_BYTES = STAGES * STAGE_BYTES + CSLOTS * CHUNK_BYTES + 1024 /* alignment slack */ + 256;
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -69,6 +72,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+// Bounded wait that ignores the abort flag (used to drain issued MMAs).
+__device__ __forceinline__ bool mbar_wait_plain(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
 }
 // Bounded wait: false if the CTA aborted or the limit ran out (then abort is set).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
@@ -131,25 +140,54 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int c0, int c1) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
+               ::"l"((uint64_t)map), "r"(smem_u32(src)), "r"(c0), "r"(c1)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// named barrier over the 128 epilogue threads that also ANDs a predicate
+__device__ __forceinline__ bool epi_bar_and(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 1, 128, pi;\n selp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0;
+}
+
+// Persistent kernel: each CTA walks tiles blockIdx.x, +gridDim.x, ...; TMEM
+// holds two accumulators so the epilogue of tile t overlaps the MMAs of
+// tile t+1; C moves through a 4-slot ring of 128 x 32 fp32 chunks with TMA
+// loads (prefetched one tile ahead) and TMA stores.
 __global__ void __launch_bounds__(THREADS, 1)
 cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                     const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
-                    float* __restrict__ C, int64_t ldc_real, int M, int Nreal, int* status) {
+                    const __grid_constant__ CUtensorMap mapC, int cx0, int cy0, int tiles_n, int total_tiles,
+                    int* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte aligned stage area (128B-swizzle atoms must start on 1024 B)
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+  unsigned char* cring = base + STAGES * STAGE_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(cring + CSLOTS * CHUNK_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* cfull = tempty + 2;
+  uint64_t* done = cfull + CSLOTS;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    mbar_init(accum, 1);
+    for (int a = 0; a < 2; ++a) { mbar_init(&tfull[a], 1); mbar_init(&tempty[a], 4); }
+    for (int c = 0; c < CSLOTS; ++c) mbar_init(&cfull[c], 1);
+    mbar_init(done, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -163,82 +201,132 @@ cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const int first = blockIdx.x, stride = gridDim.x;
 
   if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    for (int kb = 0; kb < KBLOCKS; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort)) break;
-      unsigned char* st = base + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_2d(st, &mapAhi, &full[s], kb * BK, m0);
-      tma_load_2d(st + A_TILE, &mapAlo, &full[s], kb * BK, m0);
-      tma_load_2d(st + 2 * A_TILE, &mapBhi, &full[s], kb * BK, n0);
-      tma_load_2d(st + 2 * A_TILE + B_TILE, &mapBlo, &full[s], kb * BK, n0);
+    // ---------------- TMA producer: A/B K blocks into the stage ring
+    int it = 0;
+    for (int t = first; t < total_tiles && !*abort; t += stride) {
+      const int m0 = (t / tiles_n) * BM, n0 = (t % tiles_n) * BN;
+      for (int kb = 0; kb < KBLOCKS; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (it >= STAGES && !mbar_wait(&empty[s], ((it / STAGES) - 1) & 1, abort)) break;
+        unsigned char* st = base + s * STAGE_BYTES;
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        tma_load_2d(st, &mapAhi, &full[s], kb * BK, m0);
+        tma_load_2d(st + A_TILE, &mapAlo, &full[s], kb * BK, m0);
+        tma_load_2d(st + 2 * A_TILE, &mapBhi, &full[s], kb * BK, n0);
+        tma_load_2d(st + 2 * A_TILE + B_TILE, &mapBlo, &full[s], kb * BK, n0);
+      }
     }
+    // (abort path) the last stages' loads land before the CTA may exit
+    for (int j = (it > STAGES ? it - STAGES : 0); j < it; ++j) mbar_wait_plain(&full[j % STAGES], (j / STAGES) & 1);
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
-    int issued = 0;
-    for (int kb = 0; kb < KBLOCKS; ++kb) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort)) break;
+    int it = 0, lt = 0;
+    for (int t = first; t < total_tiles && !*abort; t += stride, ++lt) {
+      const int acc = lt & 1;
+      if (lt >= 2 && !mbar_wait(&tempty[acc], ((lt >> 1) - 1) & 1, abort)) break;
       tc_fence_after();
-      const uint32_t st = smem_u32(base + s * STAGE_BYTES);
-      const uint64_t ahi = kmajor_sw128_desc(st), alo = kmajor_sw128_desc(st + A_TILE);
-      const uint64_t bhi = kmajor_sw128_desc(st + 2 * A_TILE), blo = kmajor_sw128_desc(st + 2 * A_TILE + B_TILE);
+      const uint32_t d = tmem + (uint32_t)(acc * BN);
+      bool ok = true;
+      for (int kb = 0; kb < KBLOCKS; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (!mbar_wait(&full[s], (it / STAGES) & 1, abort)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t st = smem_u32(base + s * STAGE_BYTES);
+        const uint64_t ahi = kmajor_sw128_desc(st), alo = kmajor_sw128_desc(st + A_TILE);
+        const uint64_t bhi = kmajor_sw128_desc(st + 2 * A_TILE), blo = kmajor_sw128_desc(st + 2 * A_TILE + B_TILE);
 #pragma unroll
-      for (int k = 0; k < BK / 8; ++k) {
-        const uint64_t off = (uint64_t)((k * 32) >> 4);   // 8 tf32 = 32 bytes along K
-        mma_tf32(tmem, alo + off, bhi + off, issued > 0);
-        mma_tf32(tmem, ahi + off, blo + off, 1);
-        mma_tf32(tmem, ahi + off, bhi + off, 1);
-        ++issued;
+        for (int k = 0; k < BK / 8; ++k) {
+          const uint64_t off = (uint64_t)((k * 32) >> 4);   // 8 tf32 = 32 bytes along K
+          mma_tf32(d, alo + off, bhi + off, (kb | k) != 0);
+          mma_tf32(d, ahi + off, blo + off, 1);
+          mma_tf32(d, ahi + off, bhi + off, 1);
+        }
+        mma_commit(&empty[s]);
       }
-      mma_commit(&empty[s]);
+      mma_commit(&tfull[acc]);
+      if (!ok) break;
     }
-    mma_commit(accum);   // arrives once every MMA issued above has completed
+    mma_commit(done);   // arrives once every MMA this thread issued has completed
   } else if (warp >= 4) {
-    // ---------------- epilogue
-    const int q = warp - 4;              // TMEM lanes 32q .. 32q+31
-    const int row = m0 + q * 32 + lane;
-    if (mbar_wait(accum, 0, abort)) {
+    // ---------------- epilogue: 128 threads, thread = accumulator row
+    const int q = warp - 4, r = q * 32 + lane;
+    const bool leader = (q == 0 && lane == 0);
+    const int ntiles = total_tiles > first ? (total_tiles - first + stride - 1) / stride : 0;
+    auto chunk_coords = [&](int g, int& x, int& y) {
+      const int t = first + (g / CHUNKS) * stride;
+      x = cx0 + (t % tiles_n) * BN + (g % CHUNKS) * 32;
+      y = cy0 + (t / tiles_n) * BM;
+    };
+    int issued = 0, processed = 0;   // C chunk loads issued / consumed (leader)
+    if (leader) {
+      for (int g = 0; g < CSLOTS && g < ntiles * CHUNKS; ++g, ++issued) {
+        int x, y;
+        chunk_coords(g, x, y);
+        mbar_expect_tx(&cfull[g % CSLOTS], CHUNK_BYTES);
+        tma_load_2d(cring + (g % CSLOTS) * CHUNK_BYTES, &mapC, &cfull[g % CSLOTS], x, y);
+      }
+    }
+    for (int lt = 0; lt < ntiles; ++lt) {
+      const int acc = lt & 1;
+      if (!epi_bar_and(mbar_wait(&tfull[acc], (lt >> 1) & 1, abort))) break;
       tc_fence_after();
-      float* crow = C + (int64_t)row * ldc_real;
-#pragma unroll 1
-      for (int cc = 0; cc < BN; cc += 32) {
+      bool ok = true;
+      for (int c = 0; c < CHUNKS; ++c) {
+        const int g = lt * CHUNKS + c, slot = g % CSLOTS;
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)cc, v);
-        const int col = n0 + cc;
-        if (row < M) {
-          if (col + 32 <= Nreal) {
-            float4* p = reinterpret_cast<float4*>(crow + col);
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c * 32), v);
+        if (!epi_bar_and(mbar_wait(&cfull[slot], (g / CSLOTS) & 1, abort))) { ok = false; break; }
+        unsigned char* rowp = cring + slot * CHUNK_BYTES + r * 128;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              float4 c = p[i];
-              c.x -= v[4 * i];
-              c.y -= v[4 * i + 1];
-              c.z -= v[4 * i + 2];
-              c.w -= v[4 * i + 3];
-              p[i] = c;
-            }
-          } else {
-#pragma unroll
-            for (int i = 0; i < 32; ++i)
-              if (col + i < Nreal) crow[col + i] -= v[i];
+        for (int j = 0; j < 8; ++j) {
+          float4* p = reinterpret_cast<float4*>(rowp + ((j ^ (r & 7)) << 4));
+          float4 cv = *p;
+          cv.x -= v[4 * j];
+          cv.y -= v[4 * j + 1];
+          cv.z -= v[4 * j + 2];
+          cv.w -= v[4 * j + 3];
+          *p = cv;
+        }
+        fence_async_smem();
+        epi_bar();
+        if (leader) {
+          int x, y;
+          chunk_coords(g, x, y);
+          tma_store_2d(&mapC, cring + slot * CHUNK_BYTES, x, y);
+          bulk_commit();
+          processed = g + 1;
+          const int gn = g + CSLOTS;
+          if (gn < ntiles * CHUNKS) {
+            bulk_wait_read0();   // the slot's store has read its data
+            chunk_coords(gn, x, y);
+            mbar_expect_tx(&cfull[slot], CHUNK_BYTES);
+            tma_load_2d(cring + slot * CHUNK_BYTES, &mapC, &cfull[slot], x, y);
+            issued = gn + 1;
           }
         }
       }
+      tc_fence_before();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
+      if (!ok) break;
     }
-  }
-  // drain: the accumulator barrier completes once all issued MMAs are done
-  if (threadIdx.x == 0 && *abort) {
-    mbar_wait(accum, 0, abort);
-    atomicExch(status, MGT_ERR_TIMEOUT);
+    if (leader) {
+      bulk_wait0();
+      // (abort path) prefetched chunks that were never consumed land before exit
+      for (int g = processed; g < issued; ++g) mbar_wait_plain(&cfull[g % CSLOTS], (g / CSLOTS) & 1);
+    }
   }
   tc_fence_before();
   __syncthreads();
-  tc_fence_after();
+  if (threadIdx.x == 0 && *abort) atomicExch(status, MGT_ERR_TIMEOUT);
   if (warp == 2) {
+    // every issued MMA has completed before the accumulator columns are freed
+    bool drained = (lane == 0) ? mbar_wait_plain(done, 0) : true;
+    __syncwarp();
+    (void)drained;
+    tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
@@ -268,6 +356,10 @@ __global__ void split_a_kernel(const float2* __restrict__ A, int64_t lda, int M,
 // B (K x N complex) -> B'^T hi/lo (2N x 128 fp32):
 //   row 2j   : (Br[k,j], -Bi[k,j]) for k = 0..K-1, then zeros
 //   row 2j+1 : (Bi[k,j],  Br[k,j])
+// Columns N .. (grid end) are written as zeros so that the tile columns past
+// the matrix edge accumulate exactly zero (TMA stores clip the inner
+// dimension only at 16-byte granularity; a zero update leaves those bytes as
+// they were loaded).
 __global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, float* __restrict__ Bhi,
                                float* __restrict__ Blo) {
   __shared__ float2 t[64][33];
@@ -281,7 +373,6 @@ __global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K,
   for (int idx = threadIdx.x; idx < 64 * KR; idx += blockDim.x) {
     int r = idx / KR, kr = idx - r * KR;
     int jj = r >> 1, j = j0 + jj;
-    if (j >= N) continue;
     int k = kr >> 1;
     float2 b = t[k][jj];
     float v;
@@ -326,9 +417,12 @@ static bool make_map(CUtensorMap* map, float* base, int64_t rows, int box_rows) 
 
 }  // namespace tc
 
+// rows of the B split buffers for order n: 2n plus one tile of zero padding
+static int64_t b_rows(int64_t n) { return 2 * n + tc::BN; }
+
 size_t tc_scratch_bytes(int64_t n) {
-  // Ahi, Alo: n x 128; Bhi, Blo: 2n x 128 (fp32)
-  return (size_t)(2 * n + 4 * n) * tc::KR * sizeof(float) + 4096;
+  // Ahi, Alo: n x 128; Bhi, Blo: (2n + BN) x 128 (fp32)
+  return (size_t)(2 * n + 2 * b_rows(n)) * tc::KR * sizeof(float) + 4096;
 }
 
 bool tc_available() { return tc::encode_fn() != nullptr; }
@@ -338,18 +432,44 @@ int TcPlan::init(void* scratch, int64_t nmax) {
   Ahi = (float*)b;
   Alo = Ahi + nmax * tc::KR;
   Bhi = Alo + nmax * tc::KR;
-  Blo = Bhi + 2 * nmax * tc::KR;
+  Blo = Bhi + b_rows(nmax) * tc::KR;
   this->nmax = nmax;
   bool ok = tc::make_map(&mAhi, Ahi, nmax, tc::BM) && tc::make_map(&mAlo, Alo, nmax, tc::BM) &&
-            tc::make_map(&mBhi, Bhi, 2 * nmax, tc::BN) && tc::make_map(&mBlo, Blo, 2 * nmax, tc::BN);
+            tc::make_map(&mBhi, Bhi, b_rows(nmax), tc::BN) && tc::make_map(&mBlo, Blo, b_rows(nmax), tc::BN);
   return ok ? MGT_OK : MGT_ERR_CUDA;
 }
 
-int gemm_sub_tc(const TcPlan& plan, int M, int N, int K, const float2* A, int64_t lda, const float2* B, int64_t ldb,
-                float2* C, int64_t ldc, int* status, cudaStream_t s) {
+int tc_make_cmap(CUtensorMap* map, float2* C, int64_t rows, int64_t cols, int64_t ldc) {
+  tc::EncodeTiledFn fn = tc::encode_fn();
+  if (!fn) return MGT_ERR_UNSUPPORTED;
+  if (((uintptr_t)C & 15) != 0 || (ldc & 1) != 0) return MGT_ERR_ARG;
+  cuuint64_t dims[2] = {(cuuint64_t)(2 * cols), (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * 8};
+  cuuint32_t box[2] = {32, (cuuint32_t)tc::BM};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)C, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+             ? MGT_OK
+             : MGT_ERR_CUDA;
+}
+
+static int tc_num_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  });
+  return sms;
+}
+
+int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
+                const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas) {
   if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
   if (K > 64 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
-  if ((ldc & 1) != 0) return MGT_ERR_ARG;   // float4 epilogue needs 16-byte aligned rows
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc::cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
@@ -358,14 +478,15 @@ int gemm_sub_tc(const TcPlan& plan, int M, int N, int K, const float2* A, int64_
   count_launch();
   tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, plan.Ahi, plan.Alo);
   count_launch();
-  tc::split_b_kernel<<<(N + 31) / 32, 256, 0, s>>>(B, ldb, K, N, plan.Bhi, plan.Blo);
-  const int Nreal = 2 * N;
-  dim3 grid((Nreal + tc::BN - 1) / tc::BN, (M + tc::BM - 1) / tc::BM);
-  if (grid.y > 65535) return MGT_ERR_UNSUPPORTED;
+  // cover every column of the last tile (2N rounded up to BN reals)
+  tc::split_b_kernel<<<(int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32), 256, 0, s>>>(
+      B, ldb, K, N, plan.Bhi, plan.Blo);
+  const int tiles_n = (2 * N + tc::BN - 1) / tc::BN, tiles_m = (M + tc::BM - 1) / tc::BM;
+  const int total = tiles_n * tiles_m;
+  int ctas = std::min(total, max_ctas > 0 ? max_ctas : tc_num_sms());
   count_launch();
-  tc::cgemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo,
-                                                                    reinterpret_cast<float*>(C), 2 * ldc, M, Nreal,
-                                                                    status);
+  tc::cgemm_tf32x3_kernel<<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap,
+                                                                   cx0, cy0, tiles_n, total, status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
@@ -399,6 +520,9 @@ extern "C" int mgt_cgemm_sub(int dtype, int use_tensor_cores, int64_t M, int64_t
   TcPlan plan;
   int e = plan.init((char*)work + 256, nmax);
   if (e != MGT_OK) return e;
-  return gemm_sub_tc(plan, (int)M, (int)N, (int)K, (const float2*)A, lda, (const float2*)B, ldb, (float2*)C, ldc,
-                     status, s);
+  CUtensorMap cmap;
+  e = tc_make_cmap(&cmap, (float2*)C, M, N, ldc);
+  if (e != MGT_OK) return e;
+  return gemm_sub_tc(plan, cmap, (int)M, (int)N, (int)K, (const float2*)A, lda, (const float2*)B, ldb, 0, 0, status, s,
+                     0);
 }

@@ -345,20 +345,24 @@ static int num_sms() {
 
 // Trailing update: tensor cores (tcgen05 TF32x3) for complex64 when a plan is
 // given, SIMT otherwise (complex128, or no tensor-core scratch).
-static int trailing_update(const TcPlan* tc, int M, int N, int K, const double2* A, int64_t lda, const double2* B,
-                           int64_t ldb, double2* C, int64_t ldc, int*, cudaStream_t s) {
+struct TcLU {
+  TcPlan plan;
+  CUtensorMap cmap;   // the whole matrix being factored
+};
+static int trailing_update(const TcLU* tc, int M, int N, int K, const double2* A, int64_t lda, const double2* B,
+                           int64_t ldb, double2* C, int64_t ldc, int, int*, cudaStream_t s) {
   (void)tc;
   return gemm_sub<double>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
-static int trailing_update(const TcPlan* tc, int M, int N, int K, const float2* A, int64_t lda, const float2* B,
-                           int64_t ldb, float2* C, int64_t ldc, int* status, cudaStream_t s) {
-  if (tc) return gemm_sub_tc(*tc, M, N, K, A, lda, B, ldb, C, ldc, status, s);
+static int trailing_update(const TcLU* tc, int M, int N, int K, const float2* A, int64_t lda, const float2* B,
+                           int64_t ldb, float2* C, int64_t ldc, int c0, int* status, cudaStream_t s) {
+  if (tc) return gemm_sub_tc(tc->plan, tc->cmap, M, N, K, A, lda, B, ldb, 2 * c0, c0, status, s);
   return gemm_sub<float>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
 
 template <typename T, int NB>
 static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s,
-                          const TcPlan* tc = nullptr) {
+                          const TcLU* tc = nullptr) {
   using V = cplx<T>;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -402,7 +406,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     if (rem > 0) {
       dom_begin(s);
       int e = trailing_update(tc, rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w,
-                              lda, A + (int64_t)(j0 + w) * lda + j0 + w, lda, ws.status, s);
+                              lda, A + (int64_t)(j0 + w) * lda + j0 + w, lda, j0 + w, ws.status, s);
       // algorithmic work of A22 -= L21 U12: 8 rem^2 w real flops; C read+written once, A and B read once
       dom_end(s, 8.0 * rem * (double)rem * w, sizeof(V) * (2.0 * rem * (double)rem + 2.0 * rem * (double)w));
       if (e != MGT_OK) return e;
@@ -542,9 +546,10 @@ extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t
     // tensor-core trailing update when the workspace holds its split buffers,
     // the rows are 16-byte aligned (even lda) and the driver exposes TMA maps
     if (n >= kTcMinN && (lda & 1) == 0 && work_bytes >= tc_region_offset() + tc_scratch_bytes(n) && tc_available()) {
-      TcPlan plan;
-      int e = plan.init((char*)work + tc_region_offset(), n);
-      if (e == MGT_OK) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, &plan);
+      TcLU tc;
+      int e = tc.plan.init((char*)work + tc_region_offset(), n);
+      if (e == MGT_OK) e = tc_make_cmap(&tc.cmap, (float2*)A, n, n, lda);
+      if (e == MGT_OK) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, &tc);
     }
     return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
   }

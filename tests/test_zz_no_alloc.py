@@ -35,20 +35,30 @@ def test_static_scratch_lu_matches_workspace_lu():
     from magreete_gb300 import engine as E
     lib = L.load()
     gen = torch.Generator().manual_seed(1234)
-    for n, dtype, code, tol in [(700, torch.complex128, L.MGT_C128, 1e-13), (1100, torch.complex64, L.MGT_C64, 1e-6)]:
+    # complex128: both entry points run the same FP64 kernels, so the factors agree to
+    # rounding.  complex64: the workspace entry point may run its trailing update on the
+    # tensor cores (TF32x3) while the static one stays on the FP32 pipes, so the factors
+    # agree to FP32-LU accuracy (the 1e-4 bound test_lu_random uses for complex64).
+    for n, dtype, code, tol in [(700, torch.complex128, L.MGT_C128, 1e-13), (1100, torch.complex64, L.MGT_C64, 1e-4)]:
         A = torch.randn(n, n, dtype=torch.complex128, generator=gen).to(dtype).cuda()
         ref = E.lu_factor(A.clone())          # workspace entry point
         A2 = A.clone()
         perm, info = _factor_static(lib, A2, code)
         assert info.tolist() == [0, 0]
-        assert torch.equal(perm, ref.perm)
-        err = (torch.linalg.norm(A2 - ref.lu) / torch.linalg.norm(ref.lu)).item()
-        assert err <= tol, err
-        # and the static factors solve the system
+        Ad = A.to(torch.complex128)
+        Lm = torch.tril(A2.to(torch.complex128), -1) + torch.eye(n, dtype=torch.complex128, device="cuda")
+        U = torch.triu(A2.to(torch.complex128))
+        recon = (torch.linalg.norm(Lm @ U - Ad[perm.long()]) / torch.linalg.norm(Ad)).item()
+        assert recon <= tol, recon
+        if torch.equal(perm, ref.perm):
+            err = (torch.linalg.norm(A2 - ref.lu) / torch.linalg.norm(ref.lu)).item()
+            assert err <= tol, err
+        # both factorisations solve the system to the same answer
         B = torch.randn(n, 3, dtype=torch.complex128, generator=gen).to(dtype).cuda()
-        X = E.lu_solve(E.LUFactors(A2, perm, None, code), B)
-        res = (torch.linalg.norm(A.to(torch.complex128) @ X.to(torch.complex128) - B.to(torch.complex128))
-               / torch.linalg.norm(B.to(torch.complex128))).item()
+        X = E.lu_solve(E.LUFactors(A2, perm, None, code), B).to(torch.complex128)
+        Xr = E.lu_solve(ref, B).to(torch.complex128)
+        assert (torch.linalg.norm(X - Xr) / torch.linalg.norm(Xr)).item() <= tol * 10
+        res = (torch.linalg.norm(Ad @ X - B.to(torch.complex128)) / torch.linalg.norm(B.to(torch.complex128))).item()
         assert res < (1e-11 if dtype == torch.complex128 else 1e-3)
 
 
