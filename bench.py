@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
-WORKLOAD = ("serving stream: Poisson 200 req/s, 50/50 2D-TE disk / 3D-dyadic cube, N log-uniform [500,16000], "
+WORKLOAD = ("serving stream (continuous batching, 4 requests in flight): Poisson 200 req/s, 50/50 2D-TE disk / 3D-dyadic cube, N log-uniform [500,16000], "
             "k0L U[2pi*5, 2pi*25], 1-64 RHS, 20% geometry re-queries at a new k0; mixed method refined to 1e-10; "
             "detectors 360 ring (2D) / 1024 Fibonacci sphere (3D)")
 METRIC = "solves/s (mixed-N 2D/3D request stream, refined to 1e-10 relative residual)"
@@ -49,11 +49,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--requests", type=int, default=8, help="requests per step (window)")
+    ap.add_argument("--slots", type=int, default=4, help="requests in flight in the server")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--phases", action="store_true",
                     help="print per-phase device times of the transmission configs instead of the stream bench")
+    ap.add_argument("--only", default=None, help="with --phases: one case label, e.g. 3d_N4000:mixed")
     return ap.parse_args()
 
 
@@ -224,8 +226,9 @@ def run_ours(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
+    srv = serve.Server(slots=args.slots, precision=args.precision)
     for w, di in zip(wins[:args.warmup], dev_inputs[:args.warmup]):
-        serve.serve_sequential(w, args.precision, di)
+        serve.serve_stream(w, device_inputs=di, server=srv)
     torch.cuda.synchronize()
     # ---- timed region: device-resident inputs
     clocks = ClockSampler(local)
@@ -236,7 +239,7 @@ def run_ours(args, rank, world, local):
     t0 = time.perf_counter()
     lat, iters, rres = [], [], []
     for w, di in zip(wins[args.warmup:], dev_inputs[args.warmup:]):
-        res = serve.serve_sequential(w, args.precision, di)
+        res = serve.serve_stream(w, device_inputs=di, server=srv)
         lat += [r.latency for r in res]
         iters += [r.iterations for r in res]
         rres += [r.rel_residual for r in res]
@@ -253,17 +256,21 @@ def run_ours(args, rank, world, local):
     n_req = args.steps * args.requests * world
     value = n_req / elapsed
     # ---- e2e through the public API with host buffers
+    srv.close()
     e2e = None
     if not args.no_e2e:
+        # the same windows through the public Server API with host inputs and host
+        # results: points / detectors copied in, fields copied out, inside the timed region
+        esrv = serve.Server(slots=args.slots, precision=args.precision, host_results=True)
         barrier()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        h2d = d2h = 0
         for w in wins[args.warmup:]:
-            a, b = e2e_window(w, args.precision)
-            h2d, d2h = h2d + a, d2h + b
+            serve.serve_stream(w, server=esrv)
         torch.cuda.synchronize()
         e_el = time.perf_counter() - t1
+        h2d, d2h = esrv.h2d_bytes, esrv.d2h_bytes
+        esrv.close()
         if world > 1:
             t = torch.tensor([e_el], device=dev, dtype=torch.float64)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -321,8 +328,11 @@ def run_phases(args):
 
     cases = [("2d_te_N1000", W.cfg1(), ("mixed", "fp64")), ("3d_N4000", W.cfg2(), ("mixed", "fp64")),
              ("3d_N9000", W.cube_problem(9000, 3, 15.0), ("mixed",))]
+    only = args.only.split(":") if args.only else None
     for label, prob, precs in cases:
         for prec in precs:
+            if only and (label != only[0] or prec != only[1]):
+                continue
             for rep in range(2):
                 pts, det = prob.points.to(dev), prob.detectors.to(dev)
                 coef = prob.alpha * prob.k0 ** 2

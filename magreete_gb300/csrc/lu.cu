@@ -15,6 +15,7 @@
 //      column) and solves L11 U12 = A12 for the columns right of the panel.
 //   3. trailing update A22 -= L21 U12 (a complex GEMM, gemm.cu).
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -24,58 +25,43 @@
 
 namespace mgt {
 
-constexpr int kMaxPanelBlocks = 256;
+constexpr int kMaxPanelBlocks = 160;
 constexpr int kPanelThreads = 256;
-constexpr int kPanelMinRows = 64;
+constexpr int kPanelRowsTarget = 256;   // rows per CTA the panel aims for
 constexpr size_t kPanelSmemBudget = 220 * 1024;
+constexpr int kNBmax = 64;
+// one published record per (column parity, CTA): header + candidate row + diagonal row
+constexpr size_t kRecHeader = 64;
+constexpr size_t kRecBytes = (kRecHeader + 2 * kNBmax * sizeof(double2) + 127) & ~size_t(127);
 
 // Workspace layout (byte offsets), identical for both element types.
 struct LuWsLayout {
-  size_t barrier = 0;     // 2 x u32: count, generation
   size_t status = 8;      // 2 x i32: error, info
   size_t nslot = 16;      // i32: slots written by the last panel
-  size_t cand_val = 64;   // 2 x kMaxPanelBlocks x double
-  size_t cand_idx;        // 2 x kMaxPanelBlocks x i32
-  size_t slots;           // 2*NBmax x int2 (pos, src)
-  size_t rowc;            // 2 x NBmax x complex128
-  size_t cand_row;        // 2 x kMaxPanelBlocks x NBmax x complex128
+  size_t slots = 64;      // 2*NBmax x int2 (pos, src)
+  size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
   size_t total;
-  static constexpr int NBmax = 64;
   LuWsLayout() {
-    cand_idx = cand_val + 2 * kMaxPanelBlocks * sizeof(double);
-    slots = cand_idx + 2 * kMaxPanelBlocks * sizeof(int);
-    rowc = (slots + 2 * NBmax * sizeof(int2) + 255) & ~size_t(255);
-    cand_row = rowc + 2 * NBmax * sizeof(double2);
-    total = cand_row + 2 * (size_t)kMaxPanelBlocks * NBmax * sizeof(double2);
+    records = (slots + 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
+    total = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
   }
 };
 
-template <typename V>
 struct PanelWs {
-  GridBarrier bar;
   int* status;
   int* nslot;
-  double* cand_val;
-  int* cand_idx;
   int2* slots;
-  V* rowc;
-  V* cand_row;
+  unsigned char* records;
 };
 
-template <typename V>
-static PanelWs<V> panel_ws(void* work) {
+static PanelWs panel_ws(void* work) {
   LuWsLayout L;
   char* b = (char*)work;
-  PanelWs<V> w;
-  w.bar.count = (unsigned*)(b + L.barrier);
-  w.bar.gen = (unsigned*)(b + L.barrier) + 1;
+  PanelWs w;
   w.status = (int*)(b + L.status);
   w.nslot = (int*)(b + L.nslot);
-  w.cand_val = (double*)(b + L.cand_val);
-  w.cand_idx = (int*)(b + L.cand_idx);
   w.slots = (int2*)(b + L.slots);
-  w.rowc = (V*)(b + L.rowc);
-  w.cand_row = (V*)(b + L.cand_row);
+  w.records = (unsigned char*)(b + L.records);
   return w;
 }
 
@@ -83,10 +69,32 @@ __device__ __forceinline__ bool better(double v, int i, double bv, int bi) {
   return v > bv || (v == bv && i >= 0 && (bi < 0 || i < bi));
 }
 
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Panel factorisation with partial pivoting, one cooperative launch.
+//
+// Each CTA holds a contiguous chunk of panel rows in shared memory.  Per
+// column every CTA publishes a record -- its best local pivot candidate
+// (|re|+|im|, row, row contents) and, if it owns the diagonal row, that row --
+// and releases it with a 64-bit sequence number unique to (factorisation,
+// column).  Warp 0 of every CTA then polls all records with acquire loads
+// until each carries the expected number: the records are the barrier, so a
+// column costs one publish and one poll instead of a barrier plus two reads.
+// Records alternate between two buffers by column parity; a CTA can only
+// overwrite a buffer after every CTA has published (and so finished reading)
+// the column in between.  Polls are bounded; on expiry the kernel records
+// MGT_ERR_TIMEOUT and returns.
 template <typename T, int NB>
 __global__ void __launch_bounds__(kPanelThreads)
 lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int rows_per_cta,
-                int32_t* __restrict__ perm, PanelWs<cplx<T>> ws) {
+                int32_t* __restrict__ perm, PanelWs ws, unsigned long long seq0) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* S = reinterpret_cast<V*>(smem_raw);
@@ -94,7 +102,7 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
   __shared__ V RC[NB];
   __shared__ double red_val[kPanelThreads / 32];
   __shared__ int red_idx[kPanelThreads / 32];
-  __shared__ int s_best, s_p, s_wb;
+  __shared__ int s_best, s_p, s_wb, s_fail;
   __shared__ int s_piv[NB];
   __shared__ int slot_pos[2 * NB], slot_src[2 * NB];
   __shared__ int s_nslot;
@@ -110,10 +118,13 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
     int rr = idx / NB, cc = idx - rr * NB;
     S[idx] = cc < w ? A[(int64_t)(r0 + rr) * lda + cc] : czero<V>();
   }
+  if (tid == 0) s_fail = 0;
   __syncthreads();
 
   for (int c = 0; c < w; ++c) {
     const int buf = c & 1;
+    const unsigned long long seq = seq0 + (unsigned long long)c;
+    unsigned char* my = ws.records + ((size_t)buf * kMaxPanelBlocks + bid) * kRecBytes;
     // ---- 1. local pivot candidate (rows i >= c of this chunk)
     double best = -1.0;
     int bidx = -1;
@@ -140,52 +151,81 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
       }
       if (lane == 0) {
         s_best = bidx;
-        ws.cand_val[buf * kMaxPanelBlocks + bid] = best;
-        ws.cand_idx[buf * kMaxPanelBlocks + bid] = bidx;
+        *reinterpret_cast<double*>(my + 8) = best;
+        *reinterpret_cast<int*>(my + 16) = bidx;
       }
     }
     __syncthreads();
-    // ---- publish the candidate row and (owner only) the diagonal row c
+    // ---- 2. publish: candidate row, the diagonal row (owner), then the sequence number
     {
       const int bi = s_best;
-      V* dst = ws.cand_row + ((size_t)buf * kMaxPanelBlocks + bid) * NB;
+      V* cand = reinterpret_cast<V*>(my + kRecHeader);
+      V* rowc = cand + NB;
       if (bi >= 0)
-        for (int k = tid; k < w; k += kPanelThreads) dst[k] = S[(bi - r0) * NB + k];
+        for (int k = tid; k < w; k += kPanelThreads) cand[k] = S[(bi - r0) * NB + k];
       if (c >= r0 && c < r1)
-        for (int k = tid; k < w; k += kPanelThreads) ws.rowc[buf * NB + k] = S[(c - r0) * NB + k];
-    }
-    __threadfence();
-    // ---- 2. one grid barrier per column
-    if (G > 1) {
-      if (!grid_sync(ws.bar, ws.status)) return;
-    } else {
-      __syncthreads();
-    }
-    // ---- 3. global pivot: identical choice in every CTA
-    if (warp == 0) {
-      double bv = -1.0;
-      int bi = -1, bb = -1;
-      for (int q = lane; q < G; q += 32) {
-        double v = __ldcg(ws.cand_val + buf * kMaxPanelBlocks + q);
-        int i = __ldcg(ws.cand_idx + buf * kMaxPanelBlocks + q);
-        if (better(v, i, bv, bi)) { bv = v; bi = i; bb = q; }
-      }
-#pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        double ov = __shfl_down_sync(0xffffffffu, bv, off);
-        int oi = __shfl_down_sync(0xffffffffu, bi, off);
-        int ob = __shfl_down_sync(0xffffffffu, bb, off);
-        if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; bb = ob; }
-      }
-      if (lane == 0) { s_p = bi; s_wb = bb; }
+        for (int k = tid; k < w; k += kPanelThreads) rowc[k] = S[(c - r0) * NB + k];
     }
     __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      st_release_u64(reinterpret_cast<unsigned long long*>(my), seq);
+    }
+    // ---- 3. poll every CTA's record for this column, pick the global pivot
+    if (warp == 0) {
+      unsigned seen = 0;   // bit j: record lane + 32 j observed
+      const int per = (G + 31) / 32;
+      const unsigned want = (per >= 32) ? 0xffffffffu : ((1u << per) - 1u);
+      unsigned it = 0;
+      bool ok = true;
+      while (true) {
+        for (int j = 0; j < per; ++j) {
+          const int q = lane + 32 * j;
+          if (q >= G) { seen |= 1u << j; continue; }
+          if (seen & (1u << j)) continue;
+          const unsigned char* rq = ws.records + ((size_t)buf * kMaxPanelBlocks + q) * kRecBytes;
+          if (ld_acquire_u64(reinterpret_cast<const unsigned long long*>(rq)) == seq) seen |= 1u << j;
+        }
+        if (__all_sync(0xffffffffu, seen == want)) break;
+        if (++it > kSpinLimit) { ok = false; break; }
+        if (it > 32) __nanosleep(32);
+      }
+      double bv = -1.0;
+      int bi = -1, bb = -1;
+      if (ok) {
+        for (int q = lane; q < G; q += 32) {
+          const unsigned char* rq = ws.records + ((size_t)buf * kMaxPanelBlocks + q) * kRecBytes;
+          double v = __ldcg(reinterpret_cast<const double*>(rq + 8));
+          int i = __ldcg(reinterpret_cast<const int*>(rq + 16));
+          if (better(v, i, bv, bi)) { bv = v; bi = i; bb = q; }
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+          double ov = __shfl_down_sync(0xffffffffu, bv, off);
+          int oi = __shfl_down_sync(0xffffffffu, bi, off);
+          int ob = __shfl_down_sync(0xffffffffu, bb, off);
+          if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; bb = ob; }
+        }
+      }
+      if (lane == 0) {
+        s_p = bi;
+        s_wb = bb;
+        if (!ok) { s_fail = 1; atomicExch(ws.status, MGT_ERR_TIMEOUT); }
+      }
+    }
+    __syncthreads();
+    if (s_fail) return;
     // No valid candidate anywhere (the column is all NaN): keep row c in place.
     const int p = s_p >= 0 ? s_p : c, wb = s_p >= 0 ? s_wb : -1;
+    const int owner = c / rows_per_cta;
+    const V* rec_w = reinterpret_cast<const V*>(ws.records + ((size_t)buf * kMaxPanelBlocks + max(wb, 0)) * kRecBytes +
+                                                kRecHeader);
+    const V* rec_o = reinterpret_cast<const V*>(ws.records + ((size_t)buf * kMaxPanelBlocks + owner) * kRecBytes +
+                                                kRecHeader) + NB;
     for (int k = tid; k < NB; k += kPanelThreads) {
-      V rc = k < w ? ldcg(ws.rowc + buf * NB + k) : czero<V>();
+      V rc = k < w ? ldcg(rec_o + k) : czero<V>();
       RC[k] = rc;
-      U[k] = (k < w && wb >= 0) ? ldcg(ws.cand_row + ((size_t)buf * kMaxPanelBlocks + wb) * NB + k) : rc;
+      U[k] = (k < w && wb >= 0) ? ldcg(rec_w + k) : rc;
     }
     __syncthreads();
     const V piv = U[c];
@@ -270,12 +310,14 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
 
 constexpr int kSwapCols = 32;
 
+static std::atomic<unsigned long long> g_lu_calls{0};
+
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
 template <typename T, int NB>
 __global__ void __launch_bounds__(256)
 lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int nleft_blocks,
-                    PanelWs<cplx<T>> ws) {
+                    PanelWs ws) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* buf = reinterpret_cast<V*>(smem_raw);   // [2*NB][kSwapCols]
@@ -370,14 +412,19 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     cudaFuncSetAttribute(lu_swap_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
   });
-  PanelWs<V> ws = panel_ws<V>(work);
+  PanelWs ws = panel_ws(work);
+  // sequence numbers of this factorisation's panel records: unique per call
+  // (one counter for both element types: they may share a workspace)
+  const unsigned long long call_id = g_lu_calls.fetch_add(1) + 1;
   if (cudaMemsetAsync(work, 0, 64, s) != cudaSuccess) return MGT_ERR_CUDA;
   iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n);
   count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
   for (int j0 = 0; j0 < n; j0 += NB) {
     const int w = std::min(NB, n - j0), m = n - j0;
-    int G = std::max(1, std::min(sms, (m + kPanelMinRows - 1) / kPanelMinRows));
+    const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
+    int G = (int)std::max<int64_t>({1, (m + kPanelRowsTarget - 1) / kPanelRowsTarget, min_g_smem});
+    G = std::min(G, sms);
     int rpc = (m + G - 1) / G;
     size_t smem = (size_t)rpc * NB * sizeof(V);
     if (smem > kPanelSmemBudget) return MGT_ERR_UNSUPPORTED;
@@ -392,7 +439,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
+    const unsigned long long seq0 = (call_id << 24) + (unsigned long long)j0 + 1;
+    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws, seq0) != cudaSuccess)
       return MGT_ERR_CUDA;
     count_launch();
     const int nleft = (j0 + kSwapCols - 1) / kSwapCols;

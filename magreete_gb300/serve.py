@@ -1,14 +1,26 @@
-"""Request-level solve pipeline and the serving loop.
+"""Request-level solve pipeline and the continuous-batching server.
 
 A request (``workloads.Problem``) is one coupled-dipole solve: incident
 fields at the scatterers and detectors, system assembly, LU, (refined)
 solve for all right-hand sides, and matrix-free propagation to the
 detectors -- the ``generate_source`` -> ``solve`` -> ``propagate`` sequence
 the reference driver runs per frequency (magreete.py:371-400).
+
+``Server`` keeps several requests in flight on one GPU: each of ``slots``
+worker threads owns a CUDA stream and takes the oldest waiting request as
+soon as its device memory fits in the HBM budget, so requests that arrive
+while others are running are admitted as slots and memory free up, and their
+kernels overlap on the device (a latency-bound panel factorisation of one
+request runs beside the tensor-core updates of another).  Geometries stay
+resident on the device for re-queries; a re-query at a frequency whose
+factorisation is still cached reuses it.
 """
 from __future__ import annotations
 
+import collections
+import concurrent.futures as cf
 import dataclasses
+import threading
 import time
 
 import torch
@@ -25,6 +37,7 @@ class Result:
     iterations: int = 0
     rel_residual: float = float("nan")
     latency: float = float("nan")
+    reused_factorization: bool = False
 
 
 def incident_fields(prob, pts, det):
@@ -37,34 +50,41 @@ def incident_fields(prob, pts, det):
     return E0s, E0d
 
 
-def solve_problem(prob, precision="mixed", pts=None, det=None, tol=E.DEFAULT_TOL):
+def solve_problem(prob, precision="mixed", pts=None, det=None, tol=E.DEFAULT_TOL, factorization=None):
     """Run one request on the current CUDA stream; inputs already on the device
-    when pts/det are given."""
+    when pts/det are given.  With `factorization` (an engine.SystemFactorization
+    of the same geometry and frequency) the assembly and LU are skipped."""
     dev = torch.device("cuda", torch.cuda.current_device())
     pts = prob.points.to(dev) if pts is None else pts
     det = prob.detectors.to(dev) if det is None else det
     E0s, E0d = incident_fields(prob, pts, det)
-    n = prob.n
-    R = prob.nrhs
+    n, R = prob.n, prob.nrhs
     coef = prob.alpha * prob.k0 * prob.k0
-    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
-    stats = {}
-    X = E.solve_system(prob.kind, pts, prob.k0, coef, shift, E0s.reshape(n, R).contiguous(), precision, tol,
-                       E.DEFAULT_MAX_ITER, stats)
+    B = E0s.reshape(n, R).contiguous()
+    if factorization is None:
+        shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+        stats = {}
+        X = E.solve_system(prob.kind, pts, prob.k0, coef, shift, B, precision, tol, E.DEFAULT_MAX_ITER, stats)
+        it, rr = stats.get("iterations", 0), stats.get("rel_residual", float("nan"))
+    else:
+        X = factorization.solve(B)
+        it, rr = factorization.last_iterations, factorization.last_residual
     Ed = E.propagate(prob.kind, det, pts, prob.k0, coef, X, E0d.reshape(-1, R), precision=precision)
-    return Result(X, Ed, stats.get("iterations", 0), stats.get("rel_residual", float("nan")))
+    return Result(X, Ed, it, rr if rr is not None else float("nan"), reused_factorization=factorization is not None)
 
 
 def matrix_bytes(prob, precision="mixed"):
-    """Device bytes a request holds at its peak (matrix copies + right-hand sides)."""
+    """Device bytes a request holds at its peak: the matrix copies (24 B / entry
+    mixed: complex64 LU + double-float residual copy; 16 B fp64), the
+    tensor-core split buffers (3 KB per row) and the right-hand-side blocks."""
     n, R = prob.n, prob.nrhs
     per = 16 if precision == "fp64" else 24
-    return per * n * n + 6 * 16 * n * R + (1 << 20)
+    return per * n * n + 3072 * n + 8 * 16 * n * R + (64 << 20)
 
 
 def serve_sequential(problems, precision="mixed", device_inputs=None, start=None):
-    """Serve requests one at a time in arrival order.  Returns results with
-    latency = completion - arrival (seconds from `start`)."""
+    """Serve requests one at a time in arrival order (the plain one-at-a-time
+    path).  Returns results with latency = completion - arrival."""
     start = time.perf_counter() if start is None else start
     out = []
     for i, prob in enumerate(problems):
@@ -76,4 +96,171 @@ def serve_sequential(problems, precision="mixed", device_inputs=None, start=None
         torch.cuda.current_stream().synchronize()
         res.latency = time.perf_counter() - start - prob.arrival
         out.append(res)
+    return out
+
+
+class Server:
+    """Continuous-batching solve server on one GPU.
+
+    slots:       requests in flight at once (one worker thread + CUDA stream each)
+    hbm_budget:  bytes of device memory the in-flight requests may hold
+                 (default: 85% of the free memory at start)
+    precision:   "mixed" (default) or "fp64"
+    host_results: copy each result to host memory before completing it
+    """
+
+    def __init__(self, slots=4, hbm_budget=None, precision="mixed", host_results=False, factor_cache=0):
+        if not torch.cuda.is_available():
+            raise RuntimeError("magreete_gb300.Server needs a CUDA GPU")
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        free, _ = torch.cuda.mem_get_info(self.device)
+        self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
+        self.precision = precision
+        self.host_results = host_results
+        self.in_use = 0
+        self.cv = threading.Condition()
+        self.queue = collections.deque()
+        self.closed = False
+        self.resident = collections.OrderedDict()     # geometry key -> (pts, det) on device
+        self.factors = collections.OrderedDict()      # (geometry key, k0) -> SystemFactorization
+        self.factor_cache = factor_cache
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
+        self.start = time.perf_counter()
+        self.workers = [threading.Thread(target=self._run, args=(i,), daemon=True) for i in range(slots)]
+        for w in self.workers:
+            w.start()
+
+    # ---------------------------------------------------------------- API
+    def submit(self, prob, pts=None, det=None):
+        """Queue a request; returns a Future of its Result.  pts / det: device
+        copies of the inputs when the caller already holds them."""
+        fut = cf.Future()
+        need = matrix_bytes(prob, self.precision)
+        if need > self.budget:
+            fut.set_exception(MemoryError(f"request needs {need} B, above the HBM budget of {self.budget} B"))
+            return fut
+        with self.cv:
+            self.queue.append((prob, pts, det, fut, need, time.perf_counter()))
+            self.cv.notify_all()
+        return fut
+
+    def close(self):
+        with self.cv:
+            self.closed = True
+            self.cv.notify_all()
+        for w in self.workers:
+            w.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---------------------------------------------------------------- internals
+    def _take(self):
+        with self.cv:
+            while True:
+                if self.queue:
+                    need = self.queue[0][4]
+                    # cached factorisations give way to a waiting request
+                    while self.in_use + need > self.budget and self.factors:
+                        _, old = self.factors.popitem(last=False)
+                        self.in_use -= old._held
+                    if self.in_use + need <= self.budget:
+                        self.in_use += need
+                        return self.queue.popleft()
+                elif self.closed:
+                    return None
+                self.cv.wait()
+
+    def _release(self, need):
+        with self.cv:
+            self.in_use -= need
+            self.cv.notify_all()
+
+    def _geometry(self, prob, pts, det):
+        if pts is not None and det is not None:
+            return pts, det
+        key = (prob.kind, prob.seed, prob.N)
+        with self.cv:
+            hit = self.resident.get(key)
+            if hit is not None:
+                self.resident.move_to_end(key)
+                return hit
+        pts = prob.points.to(self.device, non_blocking=False)
+        det = prob.detectors.to(self.device, non_blocking=False)
+        with self.cv:
+            self.h2d_bytes += prob.points.numel() * 8 + prob.detectors.numel() * 8
+            self.resident[key] = (pts, det)
+            while len(self.resident) > 64:
+                self.resident.popitem(last=False)
+        return pts, det
+
+    def _factorization(self, prob, pts):
+        """Cached factorisation for (geometry, k0), built on a miss.  Cached
+        factorisations count against the HBM budget until evicted."""
+        key = (prob.kind, prob.seed, prob.N, prob.k0)
+        with self.cv:
+            fac = self.factors.get(key)
+            if fac is not None:
+                self.factors.move_to_end(key)
+                return fac
+        shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+        fac = E.SystemFactorization(prob.kind, pts, prob.k0, prob.alpha * prob.k0 * prob.k0, shift, self.precision)
+        held = matrix_bytes(prob, self.precision)
+        with self.cv:
+            self.factors[key] = fac
+            fac._held = held
+            self.in_use += held
+            while len(self.factors) > self.factor_cache:
+                _, old = self.factors.popitem(last=False)
+                self.in_use -= old._held
+            self.cv.notify_all()
+        return fac
+
+    def _run(self, slot):
+        torch.cuda.set_device(self.device)
+        stream = torch.cuda.Stream(self.device)
+        with torch.cuda.stream(stream):
+            while True:
+                item = self._take()
+                if item is None:
+                    return
+                prob, pts, det, fut, need, t_submit = item
+                try:
+                    pts, det = self._geometry(prob, pts, det)
+                    fac = self._factorization(prob, pts) if self.factor_cache else None
+                    res = solve_problem(prob, self.precision, pts, det, factorization=fac)
+                    if self.host_results:
+                        res.Ek = res.Ek.cpu()
+                        res.E_det = res.E_det.cpu()
+                        with self.cv:
+                            self.d2h_bytes += (res.Ek.numel() + res.E_det.numel()) * 16
+                    stream.synchronize()
+                    res.latency = time.perf_counter() - self.start - prob.arrival
+                    self._release(need)
+                    fut.set_result(res)
+                except BaseException as e:  # noqa: BLE001 -- reported through the future
+                    self._release(need)
+                    fut.set_exception(e)
+
+
+def serve_stream(problems, slots=4, precision="mixed", device_inputs=None, host_results=False, server=None):
+    """Feed `problems` to a Server at their arrival times (seconds from now)
+    and wait for all results."""
+    own = server is None
+    srv = server or Server(slots=slots, precision=precision, host_results=host_results)
+    srv.start = time.perf_counter()
+    futs = []
+    for i, prob in enumerate(problems):
+        now = time.perf_counter() - srv.start
+        if prob.arrival > now:
+            time.sleep(prob.arrival - now)
+        pts, det = device_inputs[i] if device_inputs is not None else (None, None)
+        futs.append(srv.submit(prob, pts, det))
+    out = [f.result() for f in futs]
+    if own:
+        srv.close()
     return out
