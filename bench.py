@@ -39,7 +39,6 @@ WORKLOAD = ("serving stream (continuous batching, 4 requests in flight): Poisson
             "k0L U[2pi*5, 2pi*25], 1-64 RHS, 20% geometry re-queries at a new k0; mixed method refined to 1e-10; "
             "detectors 360 ring (2D) / 1024 Fibonacci sphere (3D)")
 METRIC = "solves/s (mixed-N 2D/3D request stream, refined to 1e-10 relative residual)"
-CPU_CAP = {"2d": 1500, "3d": 900}   # size cap of the CPU sample (N)
 
 
 def parse():
@@ -130,55 +129,96 @@ def windows(steps, warmup, per_step, rank):
 
 # ------------------------------------------------------------------ CPU (reference algorithm)
 
-def cpu_sample(problems, budget):
-    """Run the numpy/scipy port of the reference algorithm on the size-capped
-    requests of `problems` until `budget` seconds are used."""
+def cpu_request_time(prob):
+    """Seconds the numpy/scipy port of the reference algorithm takes for one
+    request: sources, complex128 solve, propagate (all host threads)."""
     from oracle import oracle as O
-    done, t_used = 0, 0.0
+    t0 = time.perf_counter()
+    pts, det = prob.points.numpy(), prob.detectors.numpy()
+    if prob.kind.startswith("2d"):
+        E0s = O.source_2d(prob.kind, "plane", pts, prob.k0, prob.thetas, 0.2)
+        E0d = O.source_2d(prob.kind, "plane", det, prob.k0, prob.thetas, 0.2)
+    else:
+        E0s = O.source_3d(prob.kind, "plane", pts, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
+        E0d = O.source_3d(prob.kind, "plane", det, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
+    Ek = O.solve(prob.kind, pts, prob.k0, prob.alpha, prob.radius, E0s)
+    O.propagate(prob.kind, pts, det, Ek, prob.k0, prob.alpha, E0d)
+    return time.perf_counter() - t0
+
+
+# calibration sizes (N) per dimension: the CPU times of the stream's larger
+# requests (minutes each) are extrapolated from these
+CPU_CAL = {"2d": (500, 1000, 1800), "3d": (300, 600, 1000)}
+
+
+def cpu_calibrate(budget):
+    """Model of the port's time per request, t(n, R) = (8/3 n^3 + 8 n^2 R) / rate + b n^2:
+    `rate` is the measured complex128 LAPACK solve rate (n = 4000, 64 RHS), b (Green's
+    matrix assembly, sources, propagation) is fitted per dimension to request
+    timings at the CPU_CAL sizes."""
+    from magreete_gb300 import workloads as W
+    rng = np.random.default_rng(0)
+    n0, r0 = 4000, 64
+    A = rng.standard_normal((n0, n0)) + 1j * rng.standard_normal((n0, n0)) + n0 * np.eye(n0)
+    B = rng.standard_normal((n0, r0)) + 0j
+    np.linalg.solve(A[:500, :500], B[:500])
+    t0 = time.perf_counter()
+    np.linalg.solve(A, B)
+    rate = (8 / 3 * n0 ** 3 + 8 * n0 ** 2 * r0) / (time.perf_counter() - t0)
+    del A
+    fits, meas = {}, []
+    t_start = time.perf_counter()
+    for dim in ("2d", "3d"):
+        xs, ys = [], []
+        for N in CPU_CAL[dim]:
+            if time.perf_counter() - t_start > budget and xs:
+                break
+            prob = (W.disk_problem(N, 17 + N, 15.0, n_angles=32) if dim == "2d"
+                    else W.cube_problem(N, 17 + N, 15.0, n_dirs=16))
+            t = cpu_request_time(prob)
+            lu = (8 / 3 * prob.n ** 3 + 8 * prob.n ** 2 * prob.nrhs) / rate
+            xs.append(float(prob.n) ** 2)
+            ys.append(max(t - lu, 0.0))
+            meas.append((dim, N, round(t, 3)))
+        fits[dim] = float(np.dot(xs, ys) / np.dot(xs, xs))
+    return {"rate": rate, "b": fits}, meas
+
+
+def cpu_predict(problems, model):
+    t = 0.0
     for prob in problems:
-        cap = CPU_CAP["2d" if prob.kind.startswith("2d") else "3d"]
-        if prob.N > cap:
-            continue
-        t0 = time.perf_counter()
-        pts, det = prob.points.numpy(), prob.detectors.numpy()
-        if prob.kind.startswith("2d"):
-            E0s = O.source_2d(prob.kind, "plane", pts, prob.k0, prob.thetas, 0.2)
-            E0d = O.source_2d(prob.kind, "plane", det, prob.k0, prob.thetas, 0.2)
-        else:
-            E0s = O.source_3d(prob.kind, "plane", pts, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
-            E0d = O.source_3d(prob.kind, "plane", det, prob.k0, prob.u.numpy(), prob.p.numpy(), 0.2)
-        Ek = O.solve(prob.kind, pts, prob.k0, prob.alpha, prob.radius, E0s)
-        O.propagate(prob.kind, pts, det, Ek, prob.k0, prob.alpha, E0d)
-        t_used += time.perf_counter() - t0
-        done += 1
-        if t_used >= budget:
-            break
-    return done, t_used
+        n, R = prob.n, prob.nrhs
+        b = model["b"]["2d" if prob.kind.startswith("2d") else "3d"]
+        t += (8 / 3 * n ** 3 + 8 * n ** 2 * R) / model["rate"] + b * n * n
+    return t
+
+
+def cpu_baseline_line(problems, budget):
+    model, meas = cpu_calibrate(budget)
+    t = cpu_predict(problems, model)
+    cores = os.cpu_count()
+    sample = (f"numpy/scipy port of the reference algorithm (complex128 solve + propagate, {cores} host threads): "
+              f"LAPACK complex128 solve rate measured at n=4000 ({model['rate'] / 1e9:.0f} GFLOP/s) and whole requests "
+              f"measured at {meas} (dim, N, seconds); each of the {len(problems)} stream requests is costed as "
+              f"(8/3 n^3 + 8 n^2 R)/rate + b n^2 with b fitted per dimension to those requests (larger requests take "
+              f"minutes each on the CPU): an extrapolation from measurements, not a measurement of every request")
+    return len(problems) / t, cores, sample
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    from magreete_gb300 import workloads as W
-    # size-capped requests are rare in a short window: each step samples a longer stretch of the stream
-    wins = [W.serving_stream(128, seed=7919 * (s + 1)) for s in range(args.warmup + args.steps)]
-    budget = max(2.0, args.cpu_budget / max(1, args.steps))
-    for w in wins[:args.warmup]:
-        cpu_sample(w[:1], 1.0)
-    tot_n, tot_t = 0, 0.0
-    for w in wins[args.warmup:]:
-        n, t = cpu_sample(w, budget)
-        tot_n, tot_t = tot_n + n, tot_t + t
-    val = tot_n / tot_t if tot_t > 0 else 0.0
-    cores = os.cpu_count()
-    sample = (f"{tot_n} requests of the stream (same generator) with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D) "
-              f"(larger requests take minutes each on CPU and are skipped, so this overstates CPU throughput); "
-              f"numpy/scipy port of the reference algorithm, complex128, {cores} host threads")
+    wins = windows(args.steps, args.warmup, args.requests, 0)
+    timed = [p for w in wins[args.warmup:] for p in w]
+    t0 = time.perf_counter()
+    val, cores, sample = cpu_baseline_line(timed, args.cpu_budget)
+    wall = time.perf_counter() - t0
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(1, args.steps),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.requests / val,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
             "data": "synthetic", "config": {"workload": WORKLOAD, "requests_per_step": args.requests},
-            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
+                             "calibration_wall_s": wall},
             "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -291,12 +331,9 @@ def run_ours(args, rank, world, local):
                 "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None}
     cpu = None
     if world == 1:
-        from magreete_gb300 import workloads as W
-        n, t = cpu_sample(W.serving_stream(256, seed=99991), args.cpu_budget)
-        cpu = {"value": n / t if t > 0 else 0.0, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{n} requests of the stream (same generator) with N <= {CPU_CAP['2d']} (2D) / {CPU_CAP['3d']} (3D); "
-                         "numpy/scipy port of the reference algorithm (complex128), all host threads; larger "
-                         "requests skipped, so this overstates CPU throughput"}
+        timed = [p for w in wins[args.warmup:] for p in w]
+        val, cores, sample = cpu_baseline_line(timed, args.cpu_budget)
+        cpu = {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample}
     lat_ms = sorted(1e3 * x for x in lat)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,

@@ -19,7 +19,7 @@ std::vector<Pending> g_pending;
 std::vector<cudaEvent_t> g_free;
 double g_ms = 0, g_flops = 0, g_bytes = 0;
 uint64_t g_dom_launches = 0;
-cudaEvent_t g_open = nullptr;
+thread_local cudaEvent_t g_open = nullptr;   // one open bracket per host thread
 
 cudaEvent_t get_event() {
   if (!g_free.empty()) {

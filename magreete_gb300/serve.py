@@ -206,7 +206,7 @@ class Server:
             fac = self.factors.get(key)
             if fac is not None:
                 self.factors.move_to_end(key)
-                return fac
+                return fac, True
         shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
         fac = E.SystemFactorization(prob.kind, pts, prob.k0, prob.alpha * prob.k0 * prob.k0, shift, self.precision)
         held = matrix_bytes(prob, self.precision)
@@ -218,7 +218,7 @@ class Server:
                 _, old = self.factors.popitem(last=False)
                 self.in_use -= old._held
             self.cv.notify_all()
-        return fac
+        return fac, False
 
     def _run(self, slot):
         torch.cuda.set_device(self.device)
@@ -231,8 +231,9 @@ class Server:
                 prob, pts, det, fut, need, t_submit = item
                 try:
                     pts, det = self._geometry(prob, pts, det)
-                    fac = self._factorization(prob, pts) if self.factor_cache else None
+                    fac, hit = self._factorization(prob, pts) if self.factor_cache else (None, False)
                     res = solve_problem(prob, self.precision, pts, det, factorization=fac)
+                    res.reused_factorization = hit
                     if self.host_results:
                         res.Ek = res.Ek.cpu()
                         res.E_det = res.E_det.cpu()
