@@ -528,10 +528,27 @@ __global__ void permute_rows_kernel(const V* __restrict__ B, int64_t ldb, const 
   if (i < n && c < nrhs) X[(int64_t)i * ldx + c] = B[(int64_t)perm[i] * ldb + c];
 }
 
+template <typename T, bool UPPER>
+int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int nrhs, void* work, int* status,
+              cudaStream_t s);
+size_t tri_solve_workspace_bytes(int64_t n);
+
 template <typename T>
 static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* perm, const cplx<T>* B,
-                         int64_t ldb, cplx<T>* X, int64_t ldx, int nrhs, cudaStream_t s) {
+                         int64_t ldb, cplx<T>* X, int64_t ldx, int nrhs, cudaStream_t s, void* work = nullptr) {
   using V = cplx<T>;
+  if (work) {
+    // persistent flag-ordered triangular solves (one launch per triangle and 64 columns)
+    if (cudaMemsetAsync(work, 0, 256, s) != cudaSuccess) return MGT_ERR_CUDA;
+    int* status = (int*)((char*)work + 128);
+    dim3 pg((nrhs + 127) / 128, n);
+    if (n > 65535) return MGT_ERR_UNSUPPORTED;
+    permute_rows_kernel<V><<<pg, 128, 0, s>>>(B, ldb, perm, X, ldx, n, nrhs);
+    count_launch();
+    int e = tri_solve<T, false>(LU, lda, X, ldx, n, nrhs, work, status, s);
+    if (e == MGT_OK) e = tri_solve<T, true>(LU, lda, X, ldx, n, nrhs, work, status, s);
+    return e;
+  }
   constexpr int BS = 64;
   static std::once_flag once;
   const size_t smem = (BS * BS + BS * kTrsmCols) * sizeof(V);
@@ -604,17 +621,25 @@ extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t
   return MGT_ERR_ARG;
 }
 
+extern "C" int mgt_lu_solve_workspace_bytes(int64_t n, size_t* bytes) {
+  if (!bytes || n <= 0) return MGT_ERR_ARG;
+  *bytes = tri_solve_workspace_bytes(n);
+  return MGT_OK;
+}
+
 extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_t* perm,
                             const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs, void* work,
                             size_t work_bytes, void* stream) {
-  (void)work; (void)work_bytes;
   if (!LU || !perm || !B || !X || n <= 0 || nrhs <= 0 || lda < n || ldb < nrhs || ldx < nrhs) return MGT_ERR_ARG;
   if (B == X) return MGT_ERR_ARG;
+  if (work && work_bytes < tri_solve_workspace_bytes(n)) return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == MGT_C128)
-    return lu_solve_impl<double>((const double2*)LU, (int)n, lda, perm, (const double2*)B, ldb, (double2*)X, ldx, (int)nrhs, s);
+    return lu_solve_impl<double>((const double2*)LU, (int)n, lda, perm, (const double2*)B, ldb, (double2*)X, ldx,
+                                 (int)nrhs, s, work);
   if (dtype == MGT_C64)
-    return lu_solve_impl<float>((const float2*)LU, (int)n, lda, perm, (const float2*)B, ldb, (float2*)X, ldx, (int)nrhs, s);
+    return lu_solve_impl<float>((const float2*)LU, (int)n, lda, perm, (const float2*)B, ldb, (float2*)X, ldx,
+                                (int)nrhs, s, work);
   return MGT_ERR_ARG;
 }
 

@@ -154,6 +154,8 @@ static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
+size_t tri_solve_workspace_bytes(int64_t n);
+
 // refinement workspace layout
 struct RefineWs {
   float4* Xs;     // n x nrhs double-float copy of X
@@ -161,6 +163,7 @@ struct RefineWs {
   float2* R32;    // n x nrhs complex64 residual / right-hand side
   float2* D32;    // n x nrhs complex64 correction
   double* norms;  // [0] = ||B||^2, [1] = ||R||^2
+  void* tri;      // triangular-solve flags
   size_t total;
   RefineWs(void* base, int64_t n, int64_t r) {
     char* b = (char*)base;
@@ -171,6 +174,7 @@ struct RefineWs {
     R32 = (float2*)take(n * r * sizeof(float2));
     D32 = (float2*)take(n * r * sizeof(float2));
     norms = (double*)take(2 * sizeof(double));
+    tri = take(tri_solve_workspace_bytes(n));
     total = off;
   }
 };
@@ -227,7 +231,8 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   // x0 = LU^-1 b in complex64
   count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(Bd, ldb, w.R32, nr, nn, nr);
-  int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
+  const size_t tri_bytes = tri_solve_workspace_bytes(n);
+  int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri, tri_bytes, stream);
   if (e != MGT_OK) return e;
   count_launch();
   c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 1);
@@ -247,7 +252,7 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
     prev = rel;
     count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
-    e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, nullptr, 0, stream);
+    e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri, tri_bytes, stream);
     if (e != MGT_OK) return e;
     count_launch();
   c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
