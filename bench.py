@@ -394,6 +394,16 @@ def run_phases(args):
                     e2 = ev()
                     X, it, rr = E.solve_refined(Mdf, f, B)
                 e3 = ev()
+                extra = {}
+                if prec == "mixed":
+                    # components of the refined solve, timed on their own
+                    t_a = ev()
+                    E.lu_solve(f, B.to(torch.complex64))
+                    t_b = ev()
+                    E.residual(Mdf, X, B)
+                    t_c = ev()
+                    torch.cuda.synchronize()
+                    extra = {"one_lu_solve_ms": t_a.elapsed_time(t_b), "one_residual_ms": t_b.elapsed_time(t_c)}
                 E.propagate(prob.kind, det, pts, prob.k0, coef, X, E0d.reshape(-1, R), precision=prec)
                 e4 = ev()
                 torch.cuda.synchronize()
@@ -407,7 +417,8 @@ def run_phases(args):
                                   "lu_tflops": 8 / 3 * n ** 3 / lu / 1e9, "solve_ms": e2.elapsed_time(e3),
                                   "refine_iterations": it, "rel_residual": rr, "propagate_ms": e3.elapsed_time(e4),
                                   "trailing_update": {"launches": dn, "ms": dms,
-                                                      "tflops": dfl / dms / 1e9 if dms else None}}), flush=True)
+                                                      "tflops": dfl / dms / 1e9 if dms else None}, **extra}),
+                      flush=True)
 
 
 def main():

@@ -124,11 +124,12 @@ int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, int32_t* pe
 /*
  * Solve A X = B with the factors of mgt_lu_factor (the ?getrs half of
  * ?gesv): X = U^-1 L^-1 P B for nrhs columns.  B is not modified.  With a
- * workspace of mgt_lu_solve_workspace_bytes(n) bytes each triangle is one
- * persistent launch (flag-ordered block rows); with work == NULL the solve
- * launches two kernels per 64-row block instead.
+ * workspace of mgt_lu_solve_workspace_bytes(dtype, n, nrhs) bytes each
+ * triangle is two launches (inverse of the 64 x 64 diagonal blocks, then one
+ * persistent flag-ordered solve over block rows and 16-column groups); with
+ * work == NULL the solve launches two kernels per 64-row block instead.
  */
-int mgt_lu_solve_workspace_bytes(int64_t n, size_t* bytes);
+int mgt_lu_solve_workspace_bytes(int dtype, int64_t n, int64_t nrhs, size_t* bytes);
 int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_t* perm,
                  const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
                  void* work, size_t work_bytes, void* stream);

@@ -42,7 +42,7 @@ SIGNATURES = {
     "mgt_lu_workspace_bytes": (_i32, [_i32, _i64, ctypes.POINTER(_sz)]),
     "mgt_lu_factor": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _sz, _vp]),
     "mgt_lu_factor_static": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _vp]),
-    "mgt_lu_solve_workspace_bytes": (_i32, [_i64, ctypes.POINTER(_sz)]),
+    "mgt_lu_solve_workspace_bytes": (_i32, [_i32, _i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_lu_solve": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_workspace_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int32), _vp]),
     "mgt_residual_workspace_bytes": (_i32, [_i64, _i64, ctypes.POINTER(_sz)]),

@@ -531,7 +531,7 @@ __global__ void permute_rows_kernel(const V* __restrict__ B, int64_t ldb, const 
 template <typename T, bool UPPER>
 int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int nrhs, void* work, int* status,
               cudaStream_t s);
-size_t tri_solve_workspace_bytes(int64_t n);
+size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem);
 
 template <typename T>
 static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* perm, const cplx<T>* B,
@@ -621,9 +621,9 @@ extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t
   return MGT_ERR_ARG;
 }
 
-extern "C" int mgt_lu_solve_workspace_bytes(int64_t n, size_t* bytes) {
-  if (!bytes || n <= 0) return MGT_ERR_ARG;
-  *bytes = tri_solve_workspace_bytes(n);
+extern "C" int mgt_lu_solve_workspace_bytes(int dtype, int64_t n, int64_t nrhs, size_t* bytes) {
+  if (!bytes || n <= 0 || nrhs <= 0 || (dtype != MGT_C128 && dtype != MGT_C64)) return MGT_ERR_ARG;
+  *bytes = tri_solve_workspace_bytes(n, nrhs, dtype == MGT_C128 ? sizeof(double2) : sizeof(float2));
   return MGT_OK;
 }
 
@@ -632,7 +632,8 @@ extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, c
                             size_t work_bytes, void* stream) {
   if (!LU || !perm || !B || !X || n <= 0 || nrhs <= 0 || lda < n || ldb < nrhs || ldx < nrhs) return MGT_ERR_ARG;
   if (B == X) return MGT_ERR_ARG;
-  if (work && work_bytes < tri_solve_workspace_bytes(n)) return MGT_ERR_WORKSPACE;
+  if (work && work_bytes < tri_solve_workspace_bytes(n, nrhs, dtype == MGT_C128 ? sizeof(double2) : sizeof(float2)))
+    return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == MGT_C128)
     return lu_solve_impl<double>((const double2*)LU, (int)n, lda, perm, (const double2*)B, ldb, (double2*)X, ldx,

@@ -154,7 +154,7 @@ static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
-size_t tri_solve_workspace_bytes(int64_t n);
+size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem);
 
 // refinement workspace layout
 struct RefineWs {
@@ -174,7 +174,7 @@ struct RefineWs {
     R32 = (float2*)take(n * r * sizeof(float2));
     D32 = (float2*)take(n * r * sizeof(float2));
     norms = (double*)take(2 * sizeof(double));
-    tri = take(tri_solve_workspace_bytes(n));
+    tri = take(tri_solve_workspace_bytes(n, r, sizeof(float2)));
     total = off;
   }
 };
@@ -231,7 +231,7 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   // x0 = LU^-1 b in complex64
   count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(Bd, ldb, w.R32, nr, nn, nr);
-  const size_t tri_bytes = tri_solve_workspace_bytes(n);
+  const size_t tri_bytes = tri_solve_workspace_bytes(n, nrhs, sizeof(float2));
   int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri, tri_bytes, stream);
   if (e != MGT_OK) return e;
   count_launch();

@@ -21,7 +21,7 @@
 namespace mgt {
 
 constexpr int kTB = 64;      // block rows
-constexpr int kTC = 64;      // right-hand-side columns per pass
+constexpr int kTG = 16;      // right-hand-side columns per chain (independent column groups)
 
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -32,119 +32,157 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+// Inverse of every 64 x 64 diagonal block of the unit lower (or upper) factor:
+// one CTA per block, identity right-hand sides, substitution in shared memory.
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(256)
-tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, cplx<T>* __restrict__ X, int64_t ldx, int n,
-                 int ncols, unsigned* counter, unsigned* flags, unsigned epoch, int* status) {
+diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* __restrict__ Inv) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* Ts = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
-  V* Xs = Ts + kTB * (kTB + 1);                      // [kTB][kTC]
-  __shared__ unsigned s_blk;
-  __shared__ int s_fail;
+  V* Xs = Ts + kTB * (kTB + 1);                      // [kTB][kTB]
   __shared__ V dinv[kTB];
-  const int tid = threadIdx.x, tr = tid >> 4, tc = tid & 15;
-  const int nb = (n + kTB - 1) / kTB;
+  const int tid = threadIdx.x, i = blockIdx.x;
+  const int r0 = i * kTB, rb = min(kTB, n - r0);
+  for (int idx = tid; idx < kTB * kTB; idx += 256) {
+    int r = idx >> 6, c = idx & 63;
+    Ts[r * (kTB + 1) + c] = (r < rb && c < rb) ? F[(int64_t)(r0 + r) * ldf + r0 + c] : czero<V>();
+    V e = czero<V>();
+    if (r == c) e.x = 1;
+    Xs[r * kTB + c] = e;
+  }
+  __syncthreads();
+  if (UPPER)
+    for (int r = tid; r < kTB; r += 256) dinv[r] = r < rb ? crecip(Ts[r * (kTB + 1) + r]) : czero<V>();
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  const int col = warp * 8 + (lane >> 2), t4 = lane & 3;   // 4 lanes per column, 64 columns
+  if (!UPPER) {
+    for (int kk = 0; kk < rb - 1; ++kk) {
+      __syncwarp();
+      const V xk = Xs[kk * kTB + col];
+      for (int r = kk + 1 + t4; r < rb; r += 4) cfms(Xs[r * kTB + col], Ts[r * (kTB + 1) + kk], xk);
+    }
+  } else {
+    for (int kk = rb - 1; kk >= 0; --kk) {
+      __syncwarp();
+      if (t4 == 0) Xs[kk * kTB + col] = cmul(Xs[kk * kTB + col], dinv[kk]);
+      __syncwarp();
+      const V xk = Xs[kk * kTB + col];
+      for (int r = t4; r < kk; r += 4) cfms(Xs[r * kTB + col], Ts[r * (kTB + 1) + kk], xk);
+    }
+  }
+  __syncthreads();
+  V* out = Inv + (int64_t)i * kTB * kTB;
+  for (int idx = tid; idx < kTB * kTB; idx += 256) out[idx] = Xs[idx];
+}
+
+// acc (64 x 16, 4 per thread: row tid/4, columns tid%4 + 4b) -= A (64 x 64, smem, padded) * Y (64 x 16, smem)
+template <typename V>
+__device__ __forceinline__ void block_gemm_sub(V (&acc)[4], const V* As, const V* Ys, int tr, int tc) {
+#pragma unroll 8
+  for (int kk = 0; kk < kTB; ++kk) {
+    const V a = As[tr * (kTB + 1) + kk];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) cfms(acc[b], a, Ys[kk * kTG + tc + 4 * b]);
+  }
+}
+
+// Persistent solve of one triangle.  Work items (block row, column group) are
+// claimed in dependency order; groups are independent chains.
+template <typename T, bool UPPER>
+__global__ void __launch_bounds__(256)
+tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
+                 cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols, unsigned* counter, unsigned* flags,
+                 unsigned epoch, int* status) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* As = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
+  V* Ys = As + kTB * (kTB + 1);                      // [kTB][kTG]
+  __shared__ unsigned s_item;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, tr = tid >> 2, tc = tid & 3;
+  const int nb = (n + kTB - 1) / kTB, ng = (ncols + kTG - 1) / kTG;
+  const unsigned items = (unsigned)nb * ng;
   while (true) {
-    if (tid == 0) { s_blk = atomicAdd(counter, 1u); s_fail = 0; }
+    if (tid == 0) { s_item = atomicAdd(counter, 1u); s_fail = 0; }
     __syncthreads();
-    const unsigned k = s_blk;
-    if (k >= (unsigned)nb) break;
-    const int i = UPPER ? nb - 1 - (int)k : (int)k;
-    const int r0 = i * kTB, rb = min(kTB, n - r0);
-    V acc[4][4];
+    const unsigned k = s_item;
+    if (k >= items) break;
+    const int kr = (int)(k / ng), g = (int)(k % ng);
+    const int i = UPPER ? nb - 1 - kr : kr;
+    const int r0 = i * kTB, rb = min(kTB, n - r0), cg = g * kTG;
+    unsigned* gflags = flags + (size_t)g * nb;
+    V acc[4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int r = tr + 16 * a, c = tc + 16 * b;
-        acc[a][b] = (r < rb && c < ncols) ? X[(int64_t)(r0 + r) * ldx + c] : czero<V>();
-      }
-    // ---- accumulate the dependencies: acc -= T[i, j] X_j, in the order the
-    // X_j complete (ascending j for L, descending j for U)
+    for (int b = 0; b < 4; ++b) {
+      const int c = cg + tc + 4 * b;
+      acc[b] = (tr < rb && c < ncols) ? X[(int64_t)(r0 + tr) * ldx + c] : czero<V>();
+    }
+    // dependencies in completion order: ascending for L, descending for U
     const int ndep = UPPER ? nb - 1 - i : i;
     for (int d = 0; d < ndep; ++d) {
       const int j = UPPER ? nb - 1 - d : d;
       const int c0 = j * kTB, cb = min(kTB, n - c0);
+      // the block of T does not depend on the flag: load it first
+      for (int idx = tid; idx < kTB * kTB; idx += 256) {
+        int r = idx >> 6, c = idx & 63;
+        As[r * (kTB + 1) + c] = (r < rb && c < cb) ? F[(int64_t)(r0 + r) * ldf + c0 + c] : czero<V>();
+      }
       if (tid == 0) {
         unsigned it = 0;
-        while (ld_acquire_u32(flags + j) != epoch) {
+        while (ld_acquire_u32(gflags + j) != epoch) {
           if (++it > kSpinLimit) { s_fail = 1; atomicExch(status, MGT_ERR_TIMEOUT); break; }
-          if (it > 16) __nanosleep(64);
+          if (it > 64) __nanosleep(32);
         }
       }
       __syncthreads();
       if (s_fail) return;
-      for (int idx = tid; idx < kTB * kTB; idx += 256) {
-        int r = idx >> 6, c = idx & 63;
-        Ts[r * (kTB + 1) + c] = (r < rb && c < cb) ? F[(int64_t)(r0 + r) * ldf + c0 + c] : czero<V>();
-      }
-      for (int idx = tid; idx < kTB * kTC; idx += 256) {
-        int r = idx >> 6, c = idx & 63;
-        Xs[r * kTC + c] = (r < cb && c < ncols) ? ldcg(X + (int64_t)(c0 + r) * ldx + c) : czero<V>();
+      for (int idx = tid; idx < kTB * kTG; idx += 256) {
+        int r = idx >> 4, c = idx & 15;
+        Ys[idx] = (r < cb && cg + c < ncols) ? ldcg(X + (int64_t)(c0 + r) * ldx + cg + c) : czero<V>();
       }
       __syncthreads();
-#pragma unroll 4
-      for (int kk = 0; kk < kTB; ++kk) {
-        V a[4], x[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a[q] = Ts[(tr + 16 * q) * (kTB + 1) + kk];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) x[q] = Xs[kk * kTC + tc + 16 * q];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int b = 0; b < 4; ++b) cfms(acc[q][b], a[q], x[b]);
-      }
+      block_gemm_sub(acc, As, Ys, tr, tc);
       __syncthreads();
     }
-    // ---- diagonal block
+    // X_i = Inv_i * acc
+    const V* inv = Inv + (int64_t)i * kTB * kTB;
     for (int idx = tid; idx < kTB * kTB; idx += 256) {
       int r = idx >> 6, c = idx & 63;
-      Ts[r * (kTB + 1) + c] = (r < rb && c < rb) ? F[(int64_t)(r0 + r) * ldf + r0 + c] : czero<V>();
+      As[r * (kTB + 1) + c] = inv[idx];
     }
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) Ys[tr * kTG + tc + 4 * b] = acc[b];
+    __syncthreads();
+    V out[4];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) Xs[(tr + 16 * a) * kTC + tc + 16 * b] = acc[a][b];
-    __syncthreads();
-    if (UPPER)
-      for (int r = tid; r < rb; r += 256) dinv[r] = crecip(Ts[r * (kTB + 1) + r]);
-    __syncthreads();
-    {
-      // 4 lanes per column, 8 columns per warp
-      const int warp = tid >> 5, lane = tid & 31;
-      const int col = warp * 8 + (lane >> 2), t4 = lane & 3;
-      if (!UPPER) {
-        for (int kk = 0; kk < rb - 1; ++kk) {
-          __syncwarp();
-          const V xk = Xs[kk * kTC + col];
-          for (int r = kk + 1 + t4; r < rb; r += 4) cfms(Xs[r * kTC + col], Ts[r * (kTB + 1) + kk], xk);
-        }
-      } else {
-        for (int kk = rb - 1; kk >= 0; --kk) {
-          __syncwarp();
-          if (t4 == 0) Xs[kk * kTC + col] = cmul(Xs[kk * kTC + col], dinv[kk]);
-          __syncwarp();
-          const V xk = Xs[kk * kTC + col];
-          for (int r = t4; r < kk; r += 4) cfms(Xs[r * kTC + col], Ts[r * (kTB + 1) + kk], xk);
-        }
+    for (int b = 0; b < 4; ++b) out[b] = czero<V>();
+    block_gemm_sub(out, As, Ys, tr, tc);   // out = -Inv * acc
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int c = cg + tc + 4 * b;
+      if (tr < rb && c < ncols) {
+        V v = out[b];
+        v.x = -v.x;
+        v.y = -v.y;
+        X[(int64_t)(r0 + tr) * ldx + c] = v;
       }
-    }
-    __syncthreads();
-    for (int idx = tid; idx < kTB * kTC; idx += 256) {
-      int r = idx >> 6, c = idx & 63;
-      if (r < rb && c < ncols) X[(int64_t)(r0 + r) * ldx + c] = Xs[r * kTC + c];
     }
     __threadfence();
     __syncthreads();
-    if (tid == 0) st_release_u32(flags + i, epoch);
+    if (tid == 0) st_release_u32(gflags + i, epoch);
   }
 }
 
 static std::atomic<unsigned> g_solve_epoch{0};
 
-size_t tri_solve_workspace_bytes(int64_t n) { return (size_t)(((n + kTB - 1) / kTB) + 64) * sizeof(unsigned) + 256; }
+// counter + status (256 B), flags (groups x blocks), inverted diagonal blocks (L and U)
+size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem) {
+  const int64_t nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG;
+  size_t flags = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
+  return 256 + flags + 2 * (size_t)nb * kTB * kTB * elem * 2;
+}
 
 static int resident_ctas(const void* kern, size_t smem) {
   int dev = 0, sms = 1, per = 1;
@@ -154,29 +192,32 @@ static int resident_ctas(const void* kern, size_t smem) {
   return std::max(1, sms * std::max(1, per));
 }
 
-// In-place X = T^-1 X for all nrhs columns (T = unit lower or upper part of F).
+// In-place X = T^-1 X (T = unit lower or upper part of F), nrhs columns.
 template <typename T, bool UPPER>
 int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int nrhs, void* work, int* status,
               cudaStream_t s) {
   using V = cplx<T>;
-  const size_t smem = (size_t)(kTB * (kTB + 1) + kTB * kTC) * sizeof(V);
+  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
+  const size_t smem = (size_t)(kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
   static int max_ctas = 0;
   static std::once_flag once;
-  std::call_once(once, [smem] {
+  std::call_once(once, [smem, smem_inv] {
+    cudaFuncSetAttribute(diag_inverse_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
     cudaFuncSetAttribute(tri_solve_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     max_ctas = resident_ctas((const void*)tri_solve_kernel<T, UPPER>, smem);
   });
-  const int nb = (n + kTB - 1) / kTB;
+  const int nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG;
   unsigned* counter = (unsigned*)work;
-  unsigned* flags = counter + 64;
-  for (int c0 = 0; c0 < nrhs; c0 += kTC) {
-    const int nc = std::min(kTC, nrhs - c0);
-    const unsigned epoch = g_solve_epoch.fetch_add(1) + 1;
-    if (cudaMemsetAsync(counter, 0, sizeof(unsigned), s) != cudaSuccess) return MGT_ERR_CUDA;
-    count_launch();
-    tri_solve_kernel<T, UPPER><<<std::min(nb, max_ctas), 256, smem, s>>>(F, ldf, X + c0, ldx, n, nc, counter, flags,
-                                                                       epoch, status);
-  }
+  unsigned* flags = (unsigned*)((char*)work + 256);
+  size_t flag_bytes = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
+  V* inv = (V*)((char*)work + 256 + flag_bytes) + (UPPER ? (size_t)nb * kTB * kTB : 0);
+  count_launch();
+  diag_inverse_kernel<T, UPPER><<<nb, 256, smem_inv, s>>>(F, ldf, n, inv);
+  const unsigned epoch = g_solve_epoch.fetch_add(1) + 1;
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned), s) != cudaSuccess) return MGT_ERR_CUDA;
+  count_launch();
+  const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
+  tri_solve_kernel<T, UPPER><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch, status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 

@@ -172,7 +172,8 @@ def lu_solve(f, B):
     B = B.contiguous()
     X = torch.empty_like(B)
     nb = ctypes.c_size_t()
-    L.check(lib.mgt_lu_solve_workspace_bytes(f.n, ctypes.byref(nb)), "mgt_lu_solve_workspace_bytes")
+    L.check(lib.mgt_lu_solve_workspace_bytes(f.dtype_code, f.n, B.shape[1], ctypes.byref(nb)),
+            "mgt_lu_solve_workspace_bytes")
     work = workspace(nb.value, B.device)
     L.check(lib.mgt_lu_solve(f.dtype_code, _ptr(f.lu), f.n, f.lu.stride(0), _ptr(f.perm), _ptr(B), B.shape[1],
                              _ptr(X), B.shape[1], B.shape[1], _ptr(work), work.numel(), _stream()), "mgt_lu_solve")
