@@ -140,7 +140,7 @@ int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_
  * Transmission2D.py:230 / Transmission3D.py:205), exposed on its own.
  * MGT_C128: FP64 SIMT.  MGT_C64 with use_tensor_cores = 0: FP32 SIMT;
  * use_tensor_cores = 1: tcgen05 kind::tf32 with hi/lo split operands
- * (TF32x3, FP32-level accuracy), K <= 64, ldc even; needs
+ * (TF32x3, FP32-level accuracy), K <= 128, ldc even; needs
  * mgt_cgemm_workspace_bytes(max(M, N)) bytes of workspace.
  */
 int mgt_cgemm_workspace_bytes(int64_t nmax, size_t* bytes);

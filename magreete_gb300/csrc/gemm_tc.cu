@@ -1,5 +1,5 @@
 // Tensor-core (tcgen05, kind::tf32) complex trailing update for the
-// complex64 LU:  C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 64.
+// complex64 LU:  C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 128.
 //
 // Complex -> real: with A stored interleaved (re, im) the row of A is a real
 // row of length 2K, and
@@ -42,8 +42,7 @@ namespace tc {
 constexpr int BM = 128;            // tile rows (M)
 constexpr int BN = 128;            // tile real columns (N') = 64 complex columns
 constexpr int BK = 32;             // fp32 elements per 128-byte swizzle row
-constexpr int KR = 128;            // real K of the split buffers (2 * 64)
-constexpr int KBLOCKS = KR / BK;   // 4
+constexpr int KR = 256;            // real K stride of the split buffers (2 * 128 complex)
 constexpr int STAGES = 2;
 constexpr uint32_t A_TILE = BM * BK * 4;   // 16 KB
 constexpr uint32_t B_TILE = BN * BK * 4;   // 16 KB
@@ -169,7 +168,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                     const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
                     const __grid_constant__ CUtensorMap mapC, int cx0, int cy0, int tiles_n, int total_tiles,
-                    int* status) {
+                    int kblocks, int* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* cring = base + STAGES * STAGE_BYTES;
@@ -208,7 +207,7 @@ cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
     int it = 0;
     for (int t = first; t < total_tiles && !*abort; t += stride) {
       const int m0 = (t / tiles_n) * BM, n0 = (t % tiles_n) * BN;
-      for (int kb = 0; kb < KBLOCKS; ++kb, ++it) {
+      for (int kb = 0; kb < kblocks; ++kb, ++it) {
         const int s = it % STAGES;
         if (it >= STAGES && !mbar_wait(&empty[s], ((it / STAGES) - 1) & 1, abort)) break;
         unsigned char* st = base + s * STAGE_BYTES;
@@ -230,7 +229,7 @@ cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
       tc_fence_after();
       const uint32_t d = tmem + (uint32_t)(acc * BN);
       bool ok = true;
-      for (int kb = 0; kb < KBLOCKS; ++kb, ++it) {
+      for (int kb = 0; kb < kblocks; ++kb, ++it) {
         const int s = it % STAGES;
         if (!mbar_wait(&full[s], (it / STAGES) & 1, abort)) { ok = false; break; }
         tc_fence_after();
@@ -337,41 +336,40 @@ __device__ __forceinline__ float tf32_rna(float x) {
   return __uint_as_float(r);
 }
 
-// A (M x K complex) -> Ahi, Alo (M x 128 fp32), zero beyond 2K.
-__global__ void split_a_kernel(const float2* __restrict__ A, int64_t lda, int M, int K, float* __restrict__ Ahi,
-                               float* __restrict__ Alo) {
+// A (M x K complex) -> Ahi, Alo (M rows, stride KR fp32): the first kcols
+// reals of each row (2K rounded up to the 32-wide K blocks), zero beyond 2K.
+__global__ void split_a_kernel(const float2* __restrict__ A, int64_t lda, int M, int K, int kcols,
+                               float* __restrict__ Ahi, float* __restrict__ Alo) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)M * KR) return;
-  int i = (int)(idx / KR), k = (int)(idx - (int64_t)i * KR);
+  if (idx >= (int64_t)M * kcols) return;
+  int i = (int)(idx / kcols), k = (int)(idx - (int64_t)i * kcols);
   float v = 0.f;
   if (k < 2 * K) {
     float2 a = A[(int64_t)i * lda + (k >> 1)];
     v = (k & 1) ? a.y : a.x;
   }
   float h = tf32_rna(v);
-  Ahi[idx] = h;
-  Alo[idx] = v - h;
+  const int64_t o = (int64_t)i * KR + k;
+  Ahi[o] = h;
+  Alo[o] = v - h;
 }
 
-// B (K x N complex) -> B'^T hi/lo (2N x 128 fp32):
-//   row 2j   : (Br[k,j], -Bi[k,j]) for k = 0..K-1, then zeros
-//   row 2j+1 : (Bi[k,j],  Br[k,j])
 // Columns N .. (grid end) are written as zeros so that the tile columns past
 // the matrix edge accumulate exactly zero (TMA stores clip the inner
 // dimension only at 16-byte granularity; a zero update leaves those bytes as
 // they were loaded).
-__global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, float* __restrict__ Bhi,
-                               float* __restrict__ Blo) {
-  __shared__ float2 t[64][33];
+__global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, int kcols,
+                               float* __restrict__ Bhi, float* __restrict__ Blo) {
+  __shared__ float2 t[128][33];
   const int j0 = blockIdx.x * 32;
-  for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < 128 * 32; idx += blockDim.x) {
     int k = idx / 32, jj = idx - k * 32;
     t[k][jj] = (k < K && j0 + jj < N) ? B[(int64_t)k * ldb + j0 + jj] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  // 64 output rows (2 per column j) x 128 reals
-  for (int idx = threadIdx.x; idx < 64 * KR; idx += blockDim.x) {
-    int r = idx / KR, kr = idx - r * KR;
+  // 64 output rows (2 per column j) x kcols reals
+  for (int idx = threadIdx.x; idx < 64 * kcols; idx += blockDim.x) {
+    int r = idx / kcols, kr = idx - r * kcols;
     int jj = r >> 1, j = j0 + jj;
     int k = kr >> 1;
     float2 b = t[k][jj];
@@ -469,24 +467,25 @@ static int tc_num_sms() {
 int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
                 const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas) {
   if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
-  if (K > 64 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc::cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
   });
-  int64_t na = (int64_t)M * tc::KR;
+  const int kblocks = (2 * K + tc::BK - 1) / tc::BK, kcols = kblocks * tc::BK;
+  int64_t na = (int64_t)M * kcols;
   count_launch();
-  tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, plan.Ahi, plan.Alo);
+  tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, kcols, plan.Ahi, plan.Alo);
   count_launch();
   // cover every column of the last tile (2N rounded up to BN reals)
   tc::split_b_kernel<<<(int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32), 256, 0, s>>>(
-      B, ldb, K, N, plan.Bhi, plan.Blo);
+      B, ldb, K, N, kcols, plan.Bhi, plan.Blo);
   const int tiles_n = (2 * N + tc::BN - 1) / tc::BN, tiles_m = (M + tc::BM - 1) / tc::BM;
   const int total = tiles_n * tiles_m;
   int ctas = std::min(total, max_ctas > 0 ? max_ctas : tc_num_sms());
   count_launch();
   tc::cgemm_tf32x3_kernel<<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap,
-                                                                   cx0, cy0, tiles_n, total, status);
+                                                                   cx0, cy0, tiles_n, total, kblocks, status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
@@ -512,7 +511,7 @@ extern "C" int mgt_cgemm_sub(int dtype, int use_tensor_cores, int64_t M, int64_t
   if (dtype != MGT_C64) return MGT_ERR_ARG;
   if (!use_tensor_cores)
     return gemm_sub<float>((int)M, (int)N, (int)K, (const float2*)A, lda, (const float2*)B, ldb, (float2*)C, ldc, s);
-  if (K > 64) return MGT_ERR_UNSUPPORTED;
+  if (K > 128) return MGT_ERR_UNSUPPORTED;
   int64_t nmax = std::max(M, N);
   if (!work || work_bytes < tc_scratch_bytes(nmax) + 256) return MGT_ERR_WORKSPACE;
   if (!tc_available()) return MGT_ERR_UNSUPPORTED;

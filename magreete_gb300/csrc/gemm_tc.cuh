@@ -25,7 +25,7 @@ bool tc_available();
 // 16-byte aligned base) viewed as fp32 (rows x 2 cols), 128 x 32 boxes.
 int tc_make_cmap(CUtensorMap* map, float2* C, int64_t rows, int64_t cols, int64_t ldc);
 
-// C -= A (M x K) * B (K x N), K <= 64, where C is the M x N block of the
+// C -= A (M x K) * B (K x N), K <= 128, where C is the M x N block of the
 // matrix described by cmap starting at fp32 column cx0 (= 2 * complex
 // column) and row cy0; the block must extend to the matrix's last row and
 // column (TMA stores are clipped there).  max_ctas <= 0: one CTA per SM.

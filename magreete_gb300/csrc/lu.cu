@@ -317,15 +317,16 @@ static std::atomic<unsigned long long> g_lu_calls{0};
 template <typename T, int NB>
 __global__ void __launch_bounds__(256)
 lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int nleft_blocks,
-                    PanelWs ws) {
+                    PanelWs ws, int do_trsm = 1) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* buf = reinterpret_cast<V*>(smem_raw);   // [2*NB][kSwapCols]
   V* L = buf + 2 * NB * kSwapCols;            // [NB][NB]
   const int tid = threadIdx.x;
-  const bool right = blockIdx.x >= nleft_blocks;
-  const int col0 = right ? j0 + w + (blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
-  const int colend = right ? n : j0;
+  const bool right_cols = blockIdx.x >= nleft_blocks;
+  const bool right = right_cols && do_trsm;   // columns right of the panel that get the solve
+  const int col0 = right_cols ? j0 + w + (blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
+  const int colend = right_cols ? n : j0;
   const int ncols = min(kSwapCols, colend - col0);
   const int m = n - j0;
   const int ns = min(*ws.nslot, 2 * NB);
@@ -365,6 +366,66 @@ lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, 
     bool moved = sl.x != sl.y;
     bool top = right && sl.x < w;
     if (cc < ncols && inb && (moved || top)) A[(int64_t)(j0 + sl.x) * lda + col0 + cc] = buf[q * kSwapCols + cc];
+  }
+}
+
+// Second inner panel of a 128-wide block, columns right of the block:
+// rows j1 .. j1+wb of those columns get the first inner panel's update
+// (B -= L_ba U_a) and then U12 = L_bb^-1 B.  The row interchanges of the
+// second panel have already been applied to every column.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256)
+lu_preupdate_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, int wa, int j1, int wb, int col_begin) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* buf = reinterpret_cast<V*>(smem_raw);    // [NB][kSwapCols]
+  V* Lba = buf + NB * kSwapCols;               // [NB][NB + 1]
+  V* Ua = Lba + NB * (NB + 1);                 // [NB][kSwapCols]
+  const int tid = threadIdx.x;
+  const int col0 = col_begin + blockIdx.x * kSwapCols;
+  const int ncols = min(kSwapCols, n - col0);
+  for (int idx = tid; idx < wb * kSwapCols; idx += 256) {
+    int r = idx / kSwapCols, cc = idx - r * kSwapCols;
+    buf[r * kSwapCols + cc] = cc < ncols ? A[(int64_t)(j1 + r) * lda + col0 + cc] : czero<V>();
+  }
+  for (int idx = tid; idx < wb * wa; idx += 256) {
+    int r = idx / wa, k = idx - r * wa;
+    Lba[r * (NB + 1) + k] = A[(int64_t)(j1 + r) * lda + J0 + k];
+  }
+  for (int idx = tid; idx < wa * kSwapCols; idx += 256) {
+    int k = idx / kSwapCols, cc = idx - k * kSwapCols;
+    Ua[k * kSwapCols + cc] = cc < ncols ? A[(int64_t)(J0 + k) * lda + col0 + cc] : czero<V>();
+  }
+  __syncthreads();
+  // buf -= Lba * Ua: thread owns column cc = tid % 32 and rows tid / 32 + 8 q
+  {
+    const int cc = tid & 31, rq = tid >> 5;
+    for (int r = rq; r < wb; r += 8) {
+      V acc = buf[r * kSwapCols + cc];
+      for (int k = 0; k < wa; ++k) cfms(acc, Lba[r * (NB + 1) + k], Ua[k * kSwapCols + cc]);
+      buf[r * kSwapCols + cc] = acc;
+    }
+  }
+  __syncthreads();
+  // L_bb (unit lower) into the Lba area, then forward substitution
+  for (int idx = tid; idx < wb * wb; idx += 256) {
+    int i = idx / wb, k = idx - i * wb;
+    Lba[i * (NB + 1) + k] = A[(int64_t)(j1 + i) * lda + j1 + k];
+  }
+  __syncthreads();
+  {
+    const int warp = tid >> 5, lane = tid & 31;
+    const int cc = warp * 4 + (lane >> 3), t8 = lane & 7;
+    for (int k = 0; k < wb - 1; ++k) {
+      __syncwarp();
+      const V xk = buf[k * kSwapCols + cc];
+      for (int i = k + 1 + t8; i < wb; i += 8) cfms(buf[i * kSwapCols + cc], Lba[i * (NB + 1) + k], xk);
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < wb * kSwapCols; idx += 256) {
+    int r = idx / kSwapCols, cc = idx - r * kSwapCols;
+    if (cc < ncols) A[(int64_t)(j1 + r) * lda + col0 + cc] = buf[r * kSwapCols + cc];
   }
 }
 
@@ -420,8 +481,12 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n);
   count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
-  for (int j0 = 0; j0 < n; j0 += NB) {
-    const int w = std::min(NB, n - j0), m = n - j0;
+  const size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
+  // one inner panel: factor columns [j0, j0+w) over rows [j0, n), then apply
+  // its interchanges to every other column (and, when do_trsm, solve L11 U12 = A12
+  // for the columns right of the panel)
+  auto panel_step = [&](int j0, int w, int do_trsm) -> int {
+    const int m = n - j0;
     const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
     int G = (int)std::max<int64_t>({1, (m + kPanelRowsTarget - 1) / kPanelRowsTarget, min_g_smem});
     G = std::min(G, sms);
@@ -446,19 +511,62 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
     const int nright = (n - j0 - w + kSwapCols - 1) / kSwapCols;
     if (nleft + nright > 0) {
-      size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
-      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, s>>>(A, lda, n, j0, w, nleft, ws);
+      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, s>>>(A, lda, n, j0, w, nleft, ws, do_trsm);
       count_launch();
     }
-    const int rem = n - j0 - w;
-    if (rem > 0) {
-      dom_begin(s);
-      int e = trailing_update(tc, rem, rem, w, A + (int64_t)(j0 + w) * lda + j0, lda, A + (int64_t)j0 * lda + j0 + w,
-                              lda, A + (int64_t)(j0 + w) * lda + j0 + w, lda, j0 + w, ws.status, s);
-      // algorithmic work of A22 -= L21 U12: 8 rem^2 w real flops; C read+written once, A and B read once
-      dom_end(s, 8.0 * rem * (double)rem * w, sizeof(V) * (2.0 * rem * (double)rem + 2.0 * rem * (double)w));
+    return MGT_OK;
+  };
+  auto update = [&](int r0, int c0, int k0, int K, int rows, int cols, bool dominant) -> int {
+    // A[r0:r0+rows, c0:c0+cols] -= A[r0:, k0:k0+K] * A[k0:k0+K, c0:]
+    if (rows <= 0 || cols <= 0) return MGT_OK;
+    if (dominant) dom_begin(s);
+    int e;
+    if (dominant)
+      e = trailing_update(tc, rows, cols, K, A + (int64_t)r0 * lda + k0, lda, A + (int64_t)k0 * lda + c0, lda,
+                          A + (int64_t)r0 * lda + c0, lda, c0, ws.status, s);
+    else
+      e = gemm_sub<T>(rows, cols, K, A + (int64_t)r0 * lda + k0, lda, A + (int64_t)k0 * lda + c0, lda,
+                      A + (int64_t)r0 * lda + c0, lda, s);
+    // algorithmic work of C -= A B: 8 rows cols K real flops; C read + written once, A and B read once
+    if (dominant)
+      dom_end(s, 8.0 * rows * (double)cols * K,
+              sizeof(V) * (2.0 * rows * (double)cols + (double)rows * K + (double)K * cols));
+    return e;
+  };
+  if (tc == nullptr) {
+    for (int j0 = 0; j0 < n; j0 += NB) {
+      const int w = std::min(NB, n - j0);
+      int e = panel_step(j0, w, 1);
+      if (e == MGT_OK) e = update(j0 + w, j0 + w, j0, w, n - j0 - w, n - j0 - w, true);
       if (e != MGT_OK) return e;
     }
+    return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+  }
+  // tensor-core path: 128-wide outer blocks made of two 64-wide inner panels,
+  // so that the trailing update runs with K = 128 (half the C traffic per flop)
+  static std::once_flag once2;
+  const size_t sm3 = (NB * kSwapCols + NB * (NB + 1) + NB * kSwapCols) * sizeof(V);
+  std::call_once(once2, [sm3] {
+    cudaFuncSetAttribute(lu_preupdate_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+  });
+  for (int J0 = 0; J0 < n; J0 += 2 * NB) {
+    const int W = std::min(2 * NB, n - J0), wa = std::min(NB, W), wb = W - wa, j1 = J0 + wa;
+    int e = panel_step(J0, wa, 1);
+    if (e != MGT_OK) return e;
+    if (wb > 0) {
+      // bring the second inner panel's columns up to date, factor it
+      e = update(j1, j1, J0, wa, n - j1, wb, false);
+      if (e == MGT_OK) e = panel_step(j1, wb, 0);
+      if (e != MGT_OK) return e;
+      const int right = n - J0 - W;
+      if (right > 0) {
+        lu_preupdate_trsm_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, sm3, s>>>(A, lda, n, J0, wa, j1,
+                                                                                             wb, J0 + W);
+        count_launch();
+      }
+    }
+    e = update(J0 + W, J0 + W, J0, W, n - J0 - W, n - J0 - W, true);
+    if (e != MGT_OK) return e;
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
