@@ -182,6 +182,23 @@ int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int64_t ldlu,
                       void* stream);
 
 /*
+ * The refinement of mgt_solve_refined as stream-ordered steps that never
+ * synchronise with the host, so a whole refined solve can be captured into a
+ * CUDA graph (the batched sweep does).  Same workspace as mgt_solve_refined.
+ *   mgt_refine_start:   X = LU^-1 B (complex64 solve, widened to complex128)
+ *   mgt_refine_correct: X += LU^-1 (B - M X), residual in double-float
+ *   mgt_refine_norms:   norms_dev[0] = ||B||_F^2, norms_dev[1] = ||B - M X||_F^2
+ *                       (device doubles; the caller reads them when it syncs)
+ */
+int mgt_refine_start(const void* LU, int64_t ldlu, const int32_t* perm, int64_t n, const void* B, int64_t ldb,
+                     void* X, int64_t ldx, int64_t nrhs, void* work, size_t work_bytes, void* stream);
+int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, int64_t ldlu, const int32_t* perm, int64_t n,
+                       const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs, void* work,
+                       size_t work_bytes, void* stream);
+int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const void* B, int64_t ldb, const void* X, int64_t ldx,
+                     int64_t nrhs, void* work, size_t work_bytes, double* norms_dev, void* stream);
+
+/*
  * Matrix-free propagation to detectors:
  *   out[m*d + a, r] = coef * sum_{j,b} G_ab(t_m - s_j) Ek[j*d + b, r] + E0[m*d + a, r]
  * G is recomputed on the fly in FP64 and never stored; the contraction runs
@@ -209,6 +226,20 @@ int mgt_propagate(int kind, int dtype, const double* targets, int64_t n_targets,
  */
 int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t n,
                     int64_t ncols, void* out, void* stream);
+
+/*
+ * Tuning knobs of the LU (no counterpart in the reference), process-wide:
+ *   MGT_TUNE_PANEL_ROWS  rows of the panel each CTA of the panel kernel aims
+ *                        for (32..4096, default 256; the shared-memory limit
+ *                        can raise the CTA count further)
+ *   MGT_TUNE_OUTER_BLOCK outer block width of the complex64 tensor-core LU,
+ *                        64 or 128 (default 128: two inner panels per block)
+ * Set by the batched sweep's autotuner; mgt_get_tuning returns the value.
+ */
+#define MGT_TUNE_PANEL_ROWS 1
+#define MGT_TUNE_OUTER_BLOCK 2
+int mgt_set_tuning(int key, int value);
+int mgt_get_tuning(int key);
 
 /*
  * Diagnostics (no counterpart in the reference, which has no GPU path):

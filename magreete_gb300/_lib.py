@@ -25,6 +25,7 @@ MGT_ERR_NOT_CONVERGED = -7
 MGT_2D_VECTOR, MGT_2D_SCALAR, MGT_3D_VECTOR, MGT_3D_SCALAR = 0, 1, 2, 3
 MGT_C128, MGT_C64, MGT_CDF = 0, 1, 2
 MGT_NAN_KEEP, MGT_NAN_FILL = 0, 1
+MGT_TUNE_PANEL_ROWS, MGT_TUNE_OUTER_BLOCK = 1, 2
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -50,12 +51,17 @@ SIGNATURES = {
     "mgt_refine_workspace_bytes": (_i32, [_i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_solve_refined": (_i32, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _f64, _i32, _vp, _sz,
                                  ctypes.POINTER(_i32), ctypes.POINTER(_f64), _vp]),
+    "mgt_refine_start": (_i32, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
+    "mgt_refine_correct": (_i32, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
+    "mgt_refine_norms": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp, _vp]),
     "mgt_propagate_workspace_bytes": (_i32, [_i32, _i64, _i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_propagate": (_i32, [_i32, _i32, _vp, _i64, _vp, _i64, _f64, _f64, _f64, _i32, _f64, _vp, _i64, _vp, _i64,
                              _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_column_dots": (_i32, [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp]),
     "mgt_cgemm_workspace_bytes": (_i32, [_i64, ctypes.POINTER(_sz)]),
     "mgt_cgemm_sub": (_i32, [_i32, _i32, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _sz, _vp]),
+    "mgt_set_tuning": (_i32, [_i32, _i32]),
+    "mgt_get_tuning": (_i32, [_i32]),
     "mgt_diag_reset": (_i32, [_i32]),
     "mgt_diag_read": (_i32, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                              ctypes.POINTER(_f64), ctypes.POINTER(_f64), ctypes.POINTER(_f64)]),

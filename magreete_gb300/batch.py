@@ -1,0 +1,218 @@
+"""Batched sweeps: many independent solves of uneven size in one CUDA-graph launch.
+
+A sweep over disorder realisations or frequencies (the driver's per-copy and
+per-k0 loops, magreete.py:114, :371) is a set of independent requests.  A
+``BatchedSweep`` groups them, preallocates every device buffer of a group,
+and captures the whole group -- incident fields, assembly, complex64 LU,
+refined solve (one correction) and the final residual norms -- into one CUDA
+graph whose instances run as concurrent branches on `branches` streams.  One
+``replay()`` then launches the group.  Instances whose certified relative
+residual is still above the tolerance after the graph get further
+corrections outside it.
+
+The autotuner (``autotune``) times the group's graph for a few settings of
+the concurrent-branch count and of the LU's panel height (rows per CTA of the
+panel kernel), keeps the fastest, and caches the choice per size bucket.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+import os
+import time
+
+import torch
+
+from . import _lib as L
+from . import engine as E
+from . import selfterm
+from . import sources as S
+
+TUNE_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "magreete_gb300_tuning.json")
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class _Instance:
+    """Device buffers of one request of a batch."""
+
+    def __init__(self, prob, dev, lib):
+        self.prob = prob
+        n, R = prob.n, prob.nrhs
+        self.pts = prob.points.to(dev)
+        ld = (n + 15) // 16 * 16
+        self.M32 = torch.empty((n, ld), dtype=torch.complex64, device=dev)[:, :n]
+        self.Mdf = torch.empty((n, n, 4), dtype=torch.float32, device=dev)
+        self.perm = torch.empty(n, dtype=torch.int32, device=dev)
+        nb = ctypes.c_size_t()
+        L.check(lib.mgt_lu_workspace_bytes(L.MGT_C64, n, ctypes.byref(nb)), "mgt_lu_workspace_bytes")
+        self.luw = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=dev)
+        L.check(lib.mgt_refine_workspace_bytes(n, R, ctypes.byref(nb)), "mgt_refine_workspace_bytes")
+        self.rw = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=dev)
+        self.B = torch.empty((n, R), dtype=torch.complex128, device=dev)
+        self.X = torch.empty((n, R), dtype=torch.complex128, device=dev)
+        self.norms = torch.zeros(2, dtype=torch.float64, device=dev)
+
+    def bytes(self):
+        return sum(t.numel() * t.element_size() for t in (self.M32, self.Mdf, self.luw, self.rw, self.B, self.X)) + \
+            self.M32.shape[0] * 16 * 8
+
+    def enqueue(self, lib, stream_ptr, corrections=1):
+        """Stream-ordered solve: sources, assembly, LU, refined solve, norms."""
+        p = self.prob
+        if p.kind.startswith("2d"):
+            E0 = S.source_2d(p.kind, "plane", self.pts, p.k0, p.thetas, 0.2)
+        else:
+            E0 = S.source_3d(p.kind, "plane", self.pts, p.k0, p.u, p.p, 0.2)
+        self.B.copy_(E0.reshape(self.B.shape))
+        n, R = p.n, p.nrhs
+        coef = complex(p.alpha * p.k0 * p.k0)
+        shift = complex(selfterm.diagonal_shift(p.kind, p.k0, p.alpha, p.radius))
+        L.check(lib.mgt_assemble_system(E.KIND_CODE[p.kind], _ptr(self.pts), p.N, float(p.k0), coef.real, coef.imag,
+                                        shift.real, shift.imag, _ptr(self.Mdf), n, L.MGT_CDF, _ptr(self.M32),
+                                        self.M32.stride(0), L.MGT_C64, stream_ptr), "mgt_assemble_system")
+        L.check(lib.mgt_lu_factor(L.MGT_C64, _ptr(self.M32), n, self.M32.stride(0), _ptr(self.perm), _ptr(self.luw),
+                                  self.luw.numel(), stream_ptr), "mgt_lu_factor")
+        L.check(lib.mgt_refine_start(_ptr(self.M32), self.M32.stride(0), _ptr(self.perm), n, _ptr(self.B), R,
+                                     _ptr(self.X), R, R, _ptr(self.rw), self.rw.numel(), stream_ptr),
+                "mgt_refine_start")
+        for _ in range(corrections):
+            self.correct(lib, stream_ptr)
+        self.measure(lib, stream_ptr)
+
+    def correct(self, lib, stream_ptr):
+        p = self.prob
+        n, R = p.n, p.nrhs
+        L.check(lib.mgt_refine_correct(_ptr(self.Mdf), n, _ptr(self.M32), self.M32.stride(0), _ptr(self.perm), n,
+                                       _ptr(self.B), R, _ptr(self.X), R, R, _ptr(self.rw), self.rw.numel(),
+                                       stream_ptr), "mgt_refine_correct")
+
+    def measure(self, lib, stream_ptr):
+        p = self.prob
+        n, R = p.n, p.nrhs
+        L.check(lib.mgt_refine_norms(_ptr(self.Mdf), n, n, _ptr(self.B), R, _ptr(self.X), R, R, _ptr(self.rw),
+                                     self.rw.numel(), ctypes.c_void_p(self.norms.data_ptr()), stream_ptr),
+                "mgt_refine_norms")
+
+    def rel_residual(self):
+        b, r = self.norms.tolist()
+        return math.sqrt(r / b) if b > 0 else math.sqrt(r)
+
+
+class BatchedSweep:
+    """One CUDA graph for a group of independent refined solves.
+
+    problems: workloads.Problem list (any kinds / sizes)
+    branches: concurrent graph branches (streams) the instances are spread over
+    """
+
+    def __init__(self, problems, branches=8, tol=E.DEFAULT_TOL, device=None):
+        self.lib = L.load()
+        self.dev = device or torch.device("cuda", torch.cuda.current_device())
+        self.tol = tol
+        self.branches = max(1, int(branches))
+        # largest first, so that the long solves start early in every branch
+        order = sorted(range(len(problems)), key=lambda i: -problems[i].n)
+        self.order = order
+        self.inst = [_Instance(problems[i], self.dev, self.lib) for i in order]
+        self.graph = None
+
+    def _enqueue_all(self):
+        main = torch.cuda.current_stream()
+        streams = [torch.cuda.Stream(self.dev) for _ in range(self.branches)]
+        for st in streams:
+            st.wait_stream(main)
+        for k, inst in enumerate(self.inst):
+            st = streams[k % self.branches]
+            with torch.cuda.stream(st):
+                inst.enqueue(self.lib, ctypes.c_void_p(st.cuda_stream))
+        for st in streams:
+            main.wait_stream(st)
+
+    def warmup(self):
+        """One eager run (initialises kernels' one-time attributes; required before capture)."""
+        self._enqueue_all()
+        torch.cuda.synchronize(self.dev)
+
+    def capture(self):
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
+            self._enqueue_all()
+        return self
+
+    def replay(self):
+        """Launch the captured group and finish stragglers eagerly.  Returns
+        (iterations beyond the graph per instance, relative residuals)."""
+        self.graph.replay()
+        torch.cuda.synchronize(self.dev)
+        extra, res = [], []
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for inst in self.inst:
+            k = 0
+            rr = inst.rel_residual()
+            while rr > self.tol and k < E.DEFAULT_MAX_ITER:
+                inst.correct(self.lib, sp)
+                inst.measure(self.lib, sp)
+                torch.cuda.synchronize(self.dev)
+                rr = inst.rel_residual()
+                k += 1
+            extra.append(k)
+            res.append(rr)
+        return extra, res
+
+    def solutions(self):
+        """Fields at the scatterers, in the order the problems were given."""
+        out = [None] * len(self.inst)
+        for pos, i in enumerate(self.order):
+            out[i] = self.inst[pos].X
+        return out
+
+
+def _bucket(problems):
+    n = max(p.n for p in problems)
+    return f"n<={2 ** math.ceil(math.log2(max(n, 2)))}"
+
+
+def autotune(problems, branch_options=(4, 8, 16), panel_rows_options=(128, 256, 512), reps=1, cache=TUNE_CACHE):
+    """Pick (branches, panel rows per CTA) for groups like `problems` by timing
+    graph replays; the choice is cached per size bucket.  Returns the dict."""
+    lib = L.load()
+    key = _bucket(problems)
+    try:
+        with open(cache) as f:
+            table = json.load(f)
+    except (OSError, ValueError):
+        table = {}
+    if key in table:
+        best = table[key]
+        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(best["panel_rows"]))
+        return best
+    results = []
+    for rows in panel_rows_options:
+        L.check(lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(rows)), "mgt_set_tuning")
+        for br in branch_options:
+            sw = BatchedSweep(problems, branches=br)
+            sw.warmup()
+            sw.capture()
+            sw.replay()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                sw.replay()
+            dt = (time.perf_counter() - t0) / reps
+            results.append({"panel_rows": rows, "branches": br, "seconds": dt})
+            del sw
+            torch.cuda.empty_cache()
+    best = min(results, key=lambda r: r["seconds"])
+    lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(best["panel_rows"]))
+    best = dict(best, candidates=results)
+    table[key] = best
+    try:
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        with open(cache, "w") as f:
+            json.dump(table, f, indent=1)
+    except OSError:
+        pass
+    return best

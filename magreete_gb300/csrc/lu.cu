@@ -27,7 +27,7 @@ namespace mgt {
 
 constexpr int kMaxPanelBlocks = 160;
 constexpr int kPanelThreads = 256;
-constexpr int kPanelRowsTarget = 256;   // rows per CTA the panel aims for
+constexpr int kPanelRowsTarget = 256;   // default rows per CTA the panel aims for
 constexpr size_t kPanelSmemBudget = 220 * 1024;
 constexpr int kNBmax = 64;
 // one published record per (column parity, CTA): header + candidate row + diagonal row
@@ -38,6 +38,7 @@ constexpr size_t kRecBytes = (kRecHeader + 2 * kNBmax * sizeof(double2) + 127) &
 struct LuWsLayout {
   size_t status = 8;      // 2 x i32: error, info
   size_t nslot = 16;      // i32: slots written by the last panel
+  size_t epoch = 40;      // u64: factorisation counter (bumped on the device, never cleared)
   size_t slots = 64;      // 2*NBmax x int2 (pos, src)
   size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
   size_t total;
@@ -50,6 +51,7 @@ struct LuWsLayout {
 struct PanelWs {
   int* status;
   int* nslot;
+  unsigned long long* epoch;
   int2* slots;
   unsigned char* records;
 };
@@ -60,6 +62,7 @@ static PanelWs panel_ws(void* work) {
   PanelWs w;
   w.status = (int*)(b + L.status);
   w.nslot = (int*)(b + L.nslot);
+  w.epoch = (unsigned long long*)(b + L.epoch);
   w.slots = (int2*)(b + L.slots);
   w.records = (unsigned char*)(b + L.records);
   return w;
@@ -94,7 +97,10 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 template <typename T, int NB>
 __global__ void __launch_bounds__(kPanelThreads)
 lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int rows_per_cta,
-                int32_t* __restrict__ perm, PanelWs ws, unsigned long long seq0) {
+                int32_t* __restrict__ perm, PanelWs ws) {
+  // record sequence numbers: unique per (factorisation, column) even when the
+  // launch is replayed from a CUDA graph, because the epoch is bumped on the device
+  const unsigned long long seq0 = (*(volatile unsigned long long*)ws.epoch << 24) + (unsigned long long)j0 + 1;
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* S = reinterpret_cast<V*>(smem_raw);
@@ -310,7 +316,9 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
 
 constexpr int kSwapCols = 32;
 
-static std::atomic<unsigned long long> g_lu_calls{0};
+// run-time tuning knobs (set by the autotuner; see mgt_set_tuning)
+static std::atomic<int> g_panel_rows{kPanelRowsTarget};
+static std::atomic<int> g_outer_block{128};
 
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
@@ -429,9 +437,11 @@ lu_preupdate_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, in
   }
 }
 
-__global__ void iota_kernel(int32_t* perm, int n) {
+// perm = identity; the factorisation epoch moves on by one
+__global__ void lu_start_kernel(int32_t* perm, int n, unsigned long long* epoch) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) perm[i] = i;
+  if (i == 0) *epoch += 1;
 }
 
 static int num_sms() {
@@ -474,11 +484,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
                          (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
   });
   PanelWs ws = panel_ws(work);
-  // sequence numbers of this factorisation's panel records: unique per call
-  // (one counter for both element types: they may share a workspace)
-  const unsigned long long call_id = g_lu_calls.fetch_add(1) + 1;
-  if (cudaMemsetAsync(work, 0, 64, s) != cudaSuccess) return MGT_ERR_CUDA;
-  iota_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n);
+  if (cudaMemsetAsync(work, 0, 32, s) != cudaSuccess) return MGT_ERR_CUDA;   // status, nslot
+  lu_start_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n, ws.epoch);
   count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
   const size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
@@ -488,7 +495,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   auto panel_step = [&](int j0, int w, int do_trsm) -> int {
     const int m = n - j0;
     const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
-    int G = (int)std::max<int64_t>({1, (m + kPanelRowsTarget - 1) / kPanelRowsTarget, min_g_smem});
+    const int rows_target = g_panel_rows.load(std::memory_order_relaxed);
+    int G = (int)std::max<int64_t>({1, (m + rows_target - 1) / rows_target, min_g_smem});
     G = std::min(G, sms);
     int rpc = (m + G - 1) / G;
     size_t smem = (size_t)rpc * NB * sizeof(V);
@@ -504,8 +512,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const unsigned long long seq0 = (call_id << 24) + (unsigned long long)j0 + 1;
-    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws, seq0) != cudaSuccess)
+    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
       return MGT_ERR_CUDA;
     count_launch();
     const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
@@ -533,7 +540,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
               sizeof(V) * (2.0 * rows * (double)cols + (double)rows * K + (double)K * cols));
     return e;
   };
-  if (tc == nullptr) {
+  if (tc == nullptr || g_outer_block.load(std::memory_order_relaxed) == NB) {
     for (int j0 = 0; j0 < n; j0 += NB) {
       const int w = std::min(NB, n - j0);
       int e = panel_step(j0, w, 1);
@@ -647,8 +654,8 @@ static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* p
   using V = cplx<T>;
   if (work) {
     // persistent flag-ordered triangular solves (one launch per triangle and 64 columns)
-    if (cudaMemsetAsync(work, 0, 256, s) != cudaSuccess) return MGT_ERR_CUDA;
     int* status = (int*)((char*)work + 128);
+    if (cudaMemsetAsync(status, 0, 2 * sizeof(int), s) != cudaSuccess) return MGT_ERR_CUDA;
     dim3 pg((nrhs + 127) / 128, n);
     if (n > 65535) return MGT_ERR_UNSUPPORTED;
     permute_rows_kernel<V><<<pg, 128, 0, s>>>(B, ldb, perm, X, ldx, n, nrhs);
@@ -824,4 +831,24 @@ extern "C" int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, 
       return MGT_ERR_CUDA;
   }
   return MGT_OK;
+}
+
+extern "C" int mgt_set_tuning(int key, int value) {
+  if (key == MGT_TUNE_PANEL_ROWS) {
+    if (value < 32 || value > 4096) return MGT_ERR_ARG;
+    g_panel_rows.store(value);
+    return MGT_OK;
+  }
+  if (key == MGT_TUNE_OUTER_BLOCK) {
+    if (value != 64 && value != 128) return MGT_ERR_ARG;
+    g_outer_block.store(value);
+    return MGT_OK;
+  }
+  return MGT_ERR_ARG;
+}
+
+extern "C" int mgt_get_tuning(int key) {
+  if (key == MGT_TUNE_PANEL_ROWS) return g_panel_rows.load();
+  if (key == MGT_TUNE_OUTER_BLOCK) return g_outer_block.load();
+  return MGT_ERR_ARG;
 }

@@ -289,3 +289,73 @@ extern "C" int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_
                                           (double2*)out);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------- stream-ordered refinement steps
+//
+// The same refinement as mgt_solve_refined, split into steps that only
+// enqueue work (no host synchronisation), so that a whole solve can be
+// captured into a CUDA graph.  The caller decides how many corrections to
+// run and reads the final norms afterwards.
+
+extern "C" int mgt_refine_start(const void* LU, int64_t ldlu, const int32_t* perm, int64_t n, const void* B,
+                                int64_t ldb, void* X, int64_t ldx, int64_t nrhs, void* work, size_t work_bytes,
+                                void* stream) {
+  if (!LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || ldlu < n || ldb < nrhs || ldx < nrhs)
+    return MGT_ERR_ARG;
+  RefineWs w(work, n, nrhs);
+  if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nn = (int)n, nr = (int)nrhs;
+  const unsigned eg = (unsigned)((n * nrhs + 255) / 256);
+  count_launch();
+  c128_to_c64_kernel<<<eg, 256, 0, s>>>((const double2*)B, ldb, w.R32, nr, nn, nr);
+  int e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri,
+                       tri_solve_workspace_bytes(n, nrhs, sizeof(float2)), stream);
+  if (e != MGT_OK) return e;
+  count_launch();
+  c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, (double2*)X, ldx, nn, nr, 1);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+extern "C" int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, int64_t ldlu, const int32_t* perm,
+                                  int64_t n, const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
+                                  void* work, size_t work_bytes, void* stream) {
+  if (!M || !LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || ldm < n || ldlu < n || ldb < nrhs ||
+      ldx < nrhs)
+    return MGT_ERR_ARG;
+  RefineWs w(work, n, nrhs);
+  if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nn = (int)n, nr = (int)nrhs;
+  const unsigned eg = (unsigned)((n * nrhs + 255) / 256);
+  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+  if (e != MGT_OK) return e;
+  count_launch();
+  c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
+  e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri,
+                   tri_solve_workspace_bytes(n, nrhs, sizeof(float2)), stream);
+  if (e != MGT_OK) return e;
+  count_launch();
+  c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, (double2*)X, ldx, nn, nr, 0);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+extern "C" int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const void* B, int64_t ldb, const void* X,
+                                int64_t ldx, int64_t nrhs, void* work, size_t work_bytes, double* norms_dev,
+                                void* stream) {
+  if (!M || !B || !X || !work || !norms_dev || n <= 0 || nrhs <= 0 || ldm < n || ldb < nrhs || ldx < nrhs)
+    return MGT_ERR_ARG;
+  RefineWs w(work, n, nrhs);
+  if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nn = (int)n, nr = (int)nrhs;
+  const int64_t tot = n * nrhs;
+  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+  if (e != MGT_OK) return e;
+  if (cudaMemsetAsync(norms_dev, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
+  count_launch(2);
+  sumsq_kernel<<<(unsigned)std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>((const double2*)B, ldb, nn, nr,
+                                                                                   norms_dev);
+  sumsq_kernel<<<(unsigned)std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, norms_dev + 1);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}

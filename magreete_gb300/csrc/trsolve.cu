@@ -12,7 +12,6 @@
 // instead of four kernel launches per block row.  No CTA waits on a row that
 // was not claimed earlier by a running CTA, so progress is guaranteed.
 #include <algorithm>
-#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -94,7 +93,10 @@ template <typename T, bool UPPER>
 __global__ void __launch_bounds__(256)
 tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
                  cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols, unsigned* counter, unsigned* flags,
-                 unsigned epoch, int* status) {
+                 const unsigned* epoch_ptr, int* status) {
+  // flag value of this solve: bumped on the device before the launch, so a
+  // replay from a CUDA graph never sees the previous run's flags as ready
+  const unsigned epoch = *(volatile const unsigned*)epoch_ptr;
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* As = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
@@ -175,7 +177,11 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
   }
 }
 
-static std::atomic<unsigned> g_solve_epoch{0};
+// counter = 0 for the work-item claims; epoch += 1
+__global__ void tri_start_kernel(unsigned* counter, unsigned* epoch) {
+  *counter = 0;
+  *epoch += 1;
+}
 
 // counter + status (256 B), flags (groups x blocks), inverted diagonal blocks (L and U)
 size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem) {
@@ -213,8 +219,9 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   V* inv = (V*)((char*)work + 256 + flag_bytes) + (UPPER ? (size_t)nb * kTB * kTB : 0);
   count_launch();
   diag_inverse_kernel<T, UPPER><<<nb, 256, smem_inv, s>>>(F, ldf, n, inv);
-  const unsigned epoch = g_solve_epoch.fetch_add(1) + 1;
-  if (cudaMemsetAsync(counter, 0, sizeof(unsigned), s) != cudaSuccess) return MGT_ERR_CUDA;
+  unsigned* epoch = counter + 1;   // never cleared: it only has to change between solves
+  count_launch();
+  tri_start_kernel<<<1, 1, 0, s>>>(counter, epoch);
   count_launch();
   const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
   tri_solve_kernel<T, UPPER><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch, status);
