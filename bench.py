@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--phases", action="store_true",
                     help="print per-phase device times of the transmission configs instead of the stream bench")
     ap.add_argument("--only", default=None, help="with --phases: one case label, e.g. 3d_N4000:mixed")
+    ap.add_argument("--sweep", type=int, default=0,
+                    help="run the batched 2D sweep with this many instances (graph replays) instead")
+    ap.add_argument("--group", type=int, default=32, help="with --sweep: instances per captured graph")
     return ap.parse_args()
 
 
@@ -437,11 +440,48 @@ def run_phases(args):
                       flush=True)
 
 
+def run_sweep(args):
+    """Batched 2D sweep (TE disk, N uniform in [500, 4000], 16 angles): groups of
+    instances captured into one CUDA graph each, concurrency and panel height
+    chosen by the autotuner on the first group; instances/s over graph replays."""
+    from magreete_gb300 import _lib, batch
+    from magreete_gb300 import workloads as W
+    _lib.load()
+    probs = W.sweep_2d(args.sweep)
+    groups = [probs[i:i + args.group] for i in range(0, len(probs), args.group)]
+    best = batch.autotune(groups[0], cache=os.path.join(ROOT, "gpurun_out", "tuning.json")
+                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else batch.TUNE_CACHE)
+    t_total, worst, extra_total, flops = 0.0, 0.0, 0, 0.0
+    for g in groups:
+        sw = batch.BatchedSweep(g, branches=best["branches"])
+        sw.warmup()
+        sw.capture()
+        sw.replay()                              # first replay: warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        extra, res = sw.replay()
+        t_total += time.perf_counter() - t0
+        worst = max(worst, max(res))
+        extra_total += sum(extra)
+        flops += sum(8 / 3 * p.n ** 3 for p in g)
+        del sw
+        torch.cuda.empty_cache()
+    print(json.dumps({"case": "batched_2d_sweep", "instances": len(probs), "group": args.group,
+                      "autotune": {k: v for k, v in best.items() if k != "candidates"},
+                      "candidates": best.get("candidates"),
+                      "seconds": t_total, "instances_per_s": len(probs) / t_total,
+                      "lu_tflops_effective": flops / t_total / 1e12, "max_rel_residual": worst,
+                      "corrections_after_graph": extra_total}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.phases:
         run_phases(args)
+        return
+    if args.sweep:
+        run_sweep(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -234,10 +234,18 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        can raise the CTA count further)
  *   MGT_TUNE_OUTER_BLOCK outer block width of the complex64 tensor-core LU,
  *                        64 or 128 (default 128: two inner panels per block)
- * Set by the batched sweep's autotuner; mgt_get_tuning returns the value.
+ *   MGT_TUNE_PANEL_MAX_CTAS  upper bound on the panel kernel's CTAs (0: one per SM)
+ *   MGT_TUNE_COOPERATIVE  1 (default): the panel kernel is a cooperative
+ *                        launch; 0: a plain launch (for CUDA-graph capture),
+ *                        where the caller keeps the CTAs of all panels that may
+ *                        run at once within the SM count (every panel CTA
+ *                        then finds an SM and no panel waits on another)
+ * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
 #define MGT_TUNE_OUTER_BLOCK 2
+#define MGT_TUNE_PANEL_MAX_CTAS 3
+#define MGT_TUNE_COOPERATIVE 4
 int mgt_set_tuning(int key, int value);
 int mgt_get_tuning(int key);
 

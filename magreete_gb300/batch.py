@@ -3,8 +3,8 @@
 A sweep over disorder realisations or frequencies (the driver's per-copy and
 per-k0 loops, magreete.py:114, :371) is a set of independent requests.  A
 ``BatchedSweep`` groups them, preallocates every device buffer of a group,
-and captures the whole group -- incident fields, assembly, complex64 LU,
-refined solve (one correction) and the final residual norms -- into one CUDA
+and captures the whole group -- assembly, complex64 LU, refined solve (one
+correction) and the final residual norms -- into one CUDA
 graph whose instances run as concurrent branches on `branches` streams.  One
 ``replay()`` then launches the group.  Instances whose certified relative
 residual is still above the tolerance after the graph get further
@@ -52,7 +52,13 @@ class _Instance:
         self.luw = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=dev)
         L.check(lib.mgt_refine_workspace_bytes(n, R, ctypes.byref(nb)), "mgt_refine_workspace_bytes")
         self.rw = torch.empty(max(nb.value, 256), dtype=torch.uint8, device=dev)
-        self.B = torch.empty((n, R), dtype=torch.complex128, device=dev)
+        # incident fields are computed once, eagerly: they hold host-to-device
+        # copies of the direction tables, which a graph capture does not allow
+        if prob.kind.startswith("2d"):
+            E0 = S.source_2d(prob.kind, "plane", self.pts, prob.k0, prob.thetas, 0.2)
+        else:
+            E0 = S.source_3d(prob.kind, "plane", self.pts, prob.k0, prob.u, prob.p, 0.2)
+        self.B = E0.reshape(n, R).contiguous()
         self.X = torch.empty((n, R), dtype=torch.complex128, device=dev)
         self.norms = torch.zeros(2, dtype=torch.float64, device=dev)
 
@@ -61,13 +67,8 @@ class _Instance:
             self.M32.shape[0] * 16 * 8
 
     def enqueue(self, lib, stream_ptr, corrections=1):
-        """Stream-ordered solve: sources, assembly, LU, refined solve, norms."""
+        """Stream-ordered solve: assembly, LU, refined solve, norms."""
         p = self.prob
-        if p.kind.startswith("2d"):
-            E0 = S.source_2d(p.kind, "plane", self.pts, p.k0, p.thetas, 0.2)
-        else:
-            E0 = S.source_3d(p.kind, "plane", self.pts, p.k0, p.u, p.p, 0.2)
-        self.B.copy_(E0.reshape(self.B.shape))
         n, R = p.n, p.nrhs
         coef = complex(p.alpha * p.k0 * p.k0)
         shift = complex(selfterm.diagonal_shift(p.kind, p.k0, p.alpha, p.radius))
@@ -113,12 +114,26 @@ class BatchedSweep:
         self.lib = L.load()
         self.dev = device or torch.device("cuda", torch.cuda.current_device())
         self.tol = tol
-        self.branches = max(1, int(branches))
+        # a panel CTA holds at most 220 KB of rows (complex64, 64 columns): the
+        # largest instance needs ceil(8 n / 440) CTAs; keep the panels of all
+        # branches within the SM count
+        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        need = max(1, math.ceil(max(p.n for p in problems) / 440))
+        self.branches = max(1, min(int(branches), sms // need))
         # largest first, so that the long solves start early in every branch
         order = sorted(range(len(problems)), key=lambda i: -problems[i].n)
         self.order = order
         self.inst = [_Instance(problems[i], self.dev, self.lib) for i in order]
         self.graph = None
+
+    def _graph_mode(self, on):
+        """Panels launched without the cooperative attribute (capturable), each
+        limited to its share of the SMs so that the panels of all branches fit
+        on the GPU at once."""
+        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        L.check(self.lib.mgt_set_tuning(L.MGT_TUNE_COOPERATIVE, 0 if on else 1), "mgt_set_tuning")
+        L.check(self.lib.mgt_set_tuning(L.MGT_TUNE_PANEL_MAX_CTAS, max(1, sms // self.branches) if on else 0),
+                "mgt_set_tuning")
 
     def _enqueue_all(self):
         main = torch.cuda.current_stream()
@@ -134,13 +149,21 @@ class BatchedSweep:
 
     def warmup(self):
         """One eager run (initialises kernels' one-time attributes; required before capture)."""
-        self._enqueue_all()
-        torch.cuda.synchronize(self.dev)
+        self._graph_mode(True)
+        try:
+            self._enqueue_all()
+            torch.cuda.synchronize(self.dev)
+        finally:
+            self._graph_mode(False)
 
     def capture(self):
         self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
-            self._enqueue_all()
+        self._graph_mode(True)
+        try:
+            with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
+                self._enqueue_all()
+        finally:
+            self._graph_mode(False)
         return self
 
     def replay(self):

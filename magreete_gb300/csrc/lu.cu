@@ -319,6 +319,8 @@ constexpr int kSwapCols = 32;
 // run-time tuning knobs (set by the autotuner; see mgt_set_tuning)
 static std::atomic<int> g_panel_rows{kPanelRowsTarget};
 static std::atomic<int> g_outer_block{128};
+static std::atomic<int> g_panel_max_ctas{0};     // 0: one per SM
+static std::atomic<int> g_cooperative{1};        // panel launched with the cooperative attribute
 
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
@@ -497,7 +499,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
     const int rows_target = g_panel_rows.load(std::memory_order_relaxed);
     int G = (int)std::max<int64_t>({1, (m + rows_target - 1) / rows_target, min_g_smem});
-    G = std::min(G, sms);
+    const int gmax = g_panel_max_ctas.load(std::memory_order_relaxed);
+    G = std::min(G, gmax > 0 ? std::min(gmax, sms) : sms);
     int rpc = (m + G - 1) / G;
     size_t smem = (size_t)rpc * NB * sizeof(V);
     if (smem > kPanelSmemBudget) return MGT_ERR_UNSUPPORTED;
@@ -511,7 +514,9 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    // Without the attribute (CUDA-graph capture of concurrent branches) the
+    // caller keeps the panels' total CTA count within the SM count instead.
+    cfg.numAttrs = g_cooperative.load(std::memory_order_relaxed) ? 1 : 0;
     if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
       return MGT_ERR_CUDA;
     count_launch();
@@ -844,11 +849,22 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_outer_block.store(value);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_PANEL_MAX_CTAS) {
+    if (value < 0 || value > 4096) return MGT_ERR_ARG;
+    g_panel_max_ctas.store(value);
+    return MGT_OK;
+  }
+  if (key == MGT_TUNE_COOPERATIVE) {
+    g_cooperative.store(value ? 1 : 0);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
 extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_PANEL_ROWS) return g_panel_rows.load();
   if (key == MGT_TUNE_OUTER_BLOCK) return g_outer_block.load();
+  if (key == MGT_TUNE_PANEL_MAX_CTAS) return g_panel_max_ctas.load();
+  if (key == MGT_TUNE_COOPERATIVE) return g_cooperative.load();
   return MGT_ERR_ARG;
 }

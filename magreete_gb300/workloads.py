@@ -134,6 +134,19 @@ def cfg2():
     return cube_problem(4000, 2, 10.0)
 
 
+def sweep_2d(count=256, seed=1000):
+    """Batched 2D sweep: `count` TE disk instances, N uniform in [500, 4000]
+    (seeded per instance), k0 L uniform in [2 pi 5, 2 pi 30], 16 angles,
+    phi = 0.05, n = 1.6."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        N = int(rng.integers(500, 4001))
+        kl = float(rng.uniform(5.0, 30.0))
+        out.append(disk_problem(N, seed + i, kl, n_angles=16))
+    return out
+
+
 def dos_frequencies_cfg1():
     return [2 * math.pi * f for f in np.arange(18.5, 22.01, 0.5)]
 
