@@ -383,13 +383,17 @@ def run_phases(args):
         return e
 
     cases = [("2d_te_N1000", W.cfg1(), ("mixed", "fp64")), ("3d_N4000", W.cfg2(), ("mixed", "fp64")),
-             ("3d_N9000", W.cube_problem(9000, 3, 15.0), ("mixed",))]
+             ("3d_N9000", W.cube_problem(9000, 3, 15.0), ("mixed",)),
+             ("3d_ball_N20000", W.cfg4(), ("mixed",))]
     only = args.only.split(":") if args.only else None
+    if only and only[0] == "dos_2d_te_N1000":
+        run_dos(only[1] if len(only) > 1 else None)
+        return
     for label, prob, precs in cases:
         for prec in precs:
             if only and (label != only[0] or prec != only[1]):
                 continue
-            for rep in range(2):
+            for rep in range(1 if label == "3d_ball_N20000" else 2):
                 pts, det = prob.points.to(dev), prob.detectors.to(dev)
                 coef = prob.alpha * prob.k0 ** 2
                 shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
@@ -428,7 +432,7 @@ def run_phases(args):
                 torch.cuda.synchronize()
                 _, dn, dms, dfl, dby = _lib.diag_read()
                 _lib.diag_reset(enable_timing=False)
-                if rep == 0:
+                if rep == 0 and label != "3d_ball_N20000":
                     continue
                 lu = e1.elapsed_time(e2)
                 print(json.dumps({"case": label, "precision": prec, "n": n, "nrhs": R,
@@ -438,6 +442,32 @@ def run_phases(args):
                                   "trailing_update": {"launches": dn, "ms": dms,
                                                       "tflops": dfl / dms / 1e9 if dms else None}, **extra}),
                       flush=True)
+
+
+def run_dos(precision=None):
+    """Mean DOS of the 2D TE N=1000 config at 8 frequencies (1000 points in the
+    disk of radius L/2), both methods; their agreement and the time per
+    frequency."""
+    from magreete_gb300 import Transmission2D_vector, _lib
+    from magreete_gb300 import workloads as W
+    _lib.load()
+    prob = W.cfg1()
+    mp = W.dos_points_cfg1()
+    out = {}
+    for prec in ((precision,) if precision else ("mixed", "fp64")):
+        s = Transmission2D_vector(prob.points.cuda(), source="plane", precision=prec)
+        s.mean_DOS_measurements(mp.cuda(), W.dos_frequencies_cfg1()[0], prob.alpha, prob.radius)
+        torch.cuda.synchronize()
+        vals, t0 = [], time.perf_counter()
+        for k0 in W.dos_frequencies_cfg1():
+            vals.append(float(s.mean_DOS_measurements(mp.cuda(), k0, prob.alpha, prob.radius)))
+        torch.cuda.synchronize()
+        out[prec] = {"dos": vals, "ms_per_frequency": 1e3 * (time.perf_counter() - t0) / len(vals)}
+    if "mixed" in out and "fp64" in out:
+        a, b = np.array(out["mixed"]["dos"]), np.array(out["fp64"]["dos"])
+        out["max_rel_diff_mixed_vs_fp64"] = float(np.max(np.abs(a - b) / np.abs(b)))
+    print(json.dumps({"case": "dos_2d_te_N1000", "frequencies": len(W.dos_frequencies_cfg1()), "points": len(mp),
+                      **out}), flush=True)
 
 
 def run_sweep(args):

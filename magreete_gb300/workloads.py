@@ -147,8 +147,29 @@ def sweep_2d(count=256, seed=1000):
     return out
 
 
+def ball_problem(N, seed, kL_over_2pi, n_ref=2.0, phi=0.1, n_dirs=64, kind="3d_vector", n_det=1024):
+    """3D dyadic in the unit ball (the large strong-scattering config): phi is
+    the volume fraction of the ball, n = 2.0."""
+    V = phi * (4 * math.pi / 3) / N
+    a = (3 * V / (4 * math.pi)) ** (1 / 3)
+    u, p = directions_3d(n_dirs)
+    return Problem(kind, ball_points(N, seed), 2 * math.pi * kL_over_2pi, complex(V * (n_ref ** 2 - 1)), a,
+                   u=u, p=p, detectors=fibonacci_sphere(n_det, 3.0), seed=seed)
+
+
+def cfg4():
+    """3D dyadic, N=20000 in the unit ball, k0 L = 2 pi 15, n=2.0, phi=0.1, 64 dirs x 2 pols."""
+    return ball_problem(20000, 4, 15.0)
+
+
 def dos_frequencies_cfg1():
+    """k0 L / 2 pi = 18.5, 19, ..., 22 (the driver's 0.5 step, magreete.py:243)."""
     return [2 * math.pi * f for f in np.arange(18.5, 22.01, 0.5)]
+
+
+def dos_points_cfg1(P=1000, seed=11):
+    """P points uniform in the disk of radius L/2 (magreete.py:877-878)."""
+    return 0.5 * disk_points(P, seed)
 
 
 def serving_stream(n_requests, seed=5, rate=200.0, n_min=500, n_max=16000, requery=0.2):
