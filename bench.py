@@ -71,6 +71,16 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """Largest value of x over the ranks of the default process group (the
+    timed region of the slowest replica); x itself with one rank."""
+    if world <= 1:
+        return float(x)
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t)
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -301,10 +311,7 @@ def run_ours(args, rank, world, local):
     _, dom_n, dom_ms, dom_flops, dom_bytes = _lib.diag_read()
     _lib.diag_reset(enable_timing=False)
     barrier()
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t)
+    elapsed = max_over_ranks(elapsed, world, dev)
     n_req = args.steps * args.requests * world
     value = n_req / elapsed
     # ---- e2e through the public API with host buffers
@@ -323,10 +330,7 @@ def run_ours(args, rank, world, local):
         e_el = time.perf_counter() - t1
         h2d, d2h = esrv.h2d_bytes, esrv.d2h_bytes
         esrv.close()
-        if world > 1:
-            t = torch.tensor([e_el], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e_el = float(t)
+        e_el = max_over_ranks(e_el, world, dev)
         e2e = {"value": n_req / e_el, "unit": "solves/s", "h2d_bytes_per_step": h2d // args.steps,
                "d2h_bytes_per_step": d2h // args.steps}
     if rank != 0:

@@ -240,12 +240,16 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        where the caller keeps the CTAs of all panels that may
  *                        run at once within the SM count (every panel CTA
  *                        then finds an SM and no panel waits on another)
+ *   MGT_TUNE_PANEL_REGISTERS  panels with at most 256 rows per CTA keep one row
+ *                        per thread in registers: 1 (default) for complex64,
+ *                        2 for both types, 0 never (rows in shared memory)
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
 #define MGT_TUNE_OUTER_BLOCK 2
 #define MGT_TUNE_PANEL_MAX_CTAS 3
 #define MGT_TUNE_COOPERATIVE 4
+#define MGT_TUNE_PANEL_REGISTERS 5
 int mgt_set_tuning(int key, int value);
 int mgt_get_tuning(int key);
 

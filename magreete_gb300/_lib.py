@@ -26,6 +26,7 @@ MGT_2D_VECTOR, MGT_2D_SCALAR, MGT_3D_VECTOR, MGT_3D_SCALAR = 0, 1, 2, 3
 MGT_C128, MGT_C64, MGT_CDF = 0, 1, 2
 MGT_NAN_KEEP, MGT_NAN_FILL = 0, 1
 MGT_TUNE_PANEL_ROWS, MGT_TUNE_OUTER_BLOCK, MGT_TUNE_PANEL_MAX_CTAS, MGT_TUNE_COOPERATIVE = 1, 2, 3, 4
+MGT_TUNE_PANEL_REGISTERS = 5
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64

@@ -314,6 +314,322 @@ lu_panel_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int 
   }
 }
 
+// Register-resident panel factorisation, one row per thread (at most 256 rows
+// per CTA).  A thread keeps the unfinished part of its row in registers,
+// shifted so that the current column is always a[0]: every register index is
+// a compile-time constant while the column loop stays a loop (small code that
+// stays in the instruction cache).  Finished columns (L or U values) go to the
+// thread's row of the shared-memory tile sL, which also stages the coalesced
+// load and store of the panel.
+//
+// Pivot search without floating-point compares (FP64 is slow on this part):
+// the bits of a non-negative float / double are ordered like its value, so
+// |re|+|im| is compared as an unsigned key (bits + 1; 0 = no candidate, NaN
+// never a candidate), ties going to the lowest row -- LAPACK's i?amax rule.
+//
+// Exchange per column: each CTA publishes its best candidate row (and the
+// owner of row c publishes row c) in its record, then one flag word.  For
+// complex64 the flag word carries the candidate itself -- [tag:8 | row+1:24 |
+// key:32], tag = ((j0 + c) mod 128) + 1 -- so the pivot is known as soon as
+// every flag has been seen; flags are cleared when a factorisation starts, and
+// the previous value of a record's flag (the column two back) never carries
+// the current tag.  complex128 keeps the 64-bit sequence flag (factorisation
+// epoch, column) with the candidate in the record header.
+template <typename T>
+struct PanelKey;
+template <>
+struct PanelKey<float> {
+  using K = unsigned;
+  static constexpr bool kPacked = true;
+  __device__ static K key(float v) {
+    const unsigned u = __float_as_uint(v);
+    return u <= 0x7F800000u ? u + 1u : 0u;   // +0 .. +inf; NaN and negatives excluded
+  }
+};
+template <>
+struct PanelKey<double> {
+  using K = unsigned long long;
+  static constexpr bool kPacked = false;
+  __device__ static K key(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return u <= 0x7FF0000000000000ull ? u + 1ull : 0ull;
+  }
+};
+
+// Warp-wide argmax of (key, row): largest key, lowest row; every lane gets it.
+__device__ __forceinline__ void warp_argmax(unsigned& k, int& i) {
+  const unsigned m = __reduce_max_sync(0xffffffffu, k);
+  i = (int)__reduce_min_sync(0xffffffffu, k == m ? (unsigned)i : 0x7fffffffu);
+  k = m;
+}
+__device__ __forceinline__ void warp_argmax(unsigned long long& k, int& i) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, off);
+    if (ok > k || (ok == k && oi < i)) { k = ok; i = oi; }
+  }
+}
+
+__device__ __forceinline__ unsigned long long pack_flag(unsigned tag, int idx, unsigned key) {
+  return ((unsigned long long)tag << 56) | ((unsigned long long)(unsigned)(idx + 1) << 32) | (unsigned long long)key;
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kPanelThreads, 1)
+lu_panel_reg_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, int rows_per_cta,
+                    int32_t* __restrict__ perm, PanelWs ws) {
+  using V = cplx<T>;
+  using PK = PanelKey<T>;
+  using K = typename PK::K;
+  constexpr int LD = NB + 1;                 // padded row of sL (bank spread)
+  constexpr int kNone = 0x7fffffff;
+  constexpr int kChunk = NB < 16 ? NB : 16;   // live-column granularity of the register loops
+  extern __shared__ __align__(16) unsigned char panel_smem[];
+  V* sL = reinterpret_cast<V*>(panel_smem);
+  __shared__ V U[2 * NB];                    // pivot row, zero beyond w
+  __shared__ V RC[2 * NB];                   // row c before the interchange, zero beyond w
+  __shared__ K red_key[kPanelThreads / 32];
+  __shared__ int red_idx[kPanelThreads / 32];
+  __shared__ K s_bkey;
+  __shared__ int s_best, s_p, s_fail;
+  __shared__ int s_piv[NB];
+  __shared__ int slot_pos[2 * NB], slot_src[2 * NB];
+  __shared__ int s_nslot;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nwarps = kPanelThreads / 32;
+  const int G = gridDim.x, bid = blockIdx.x;
+  const int r0 = bid * rows_per_cta;
+  const int nr = max(0, min(m, r0 + rows_per_cta) - r0);
+  const int row = r0 + tid;
+  const bool have = tid < nr;
+  const unsigned long long seq0 = (*(volatile unsigned long long*)ws.epoch << 24) + (unsigned long long)j0 + 1;
+
+  for (int i = tid; i < 2 * NB; i += kPanelThreads) {
+    U[i] = czero<V>();
+    RC[i] = czero<V>();
+  }
+  for (int i = tid; i < nr * NB; i += kPanelThreads) {
+    const int r = i / NB, k = i % NB;
+    sL[r * LD + k] = k < w ? A[(int64_t)(r0 + r) * lda + k] : czero<V>();
+  }
+  if (tid == 0) s_fail = 0;
+  __syncthreads();
+  V a[NB];
+#pragma unroll
+  for (int k = 0; k < NB; ++k) a[k] = have ? sL[tid * LD + k] : czero<V>();
+
+  for (int c = 0; c < w; ++c) {
+    const int buf = c & 1;
+    unsigned char* my = ws.records + ((size_t)buf * kMaxPanelBlocks + bid) * kRecBytes;
+    // ---- 1. this CTA's candidate
+    K key = (have && row >= c) ? PK::key(cabs1(a[0])) : K(0);
+    int bidx = key ? row : kNone;
+    warp_argmax(key, bidx);
+    if (lane == 0) { red_key[warp] = key; red_idx[warp] = bidx; }
+    __syncthreads();
+    if (warp == 0) {
+      key = lane < nwarps ? red_key[lane] : K(0);
+      bidx = lane < nwarps ? red_idx[lane] : kNone;
+      warp_argmax(key, bidx);
+      if (lane == 0) {
+        s_best = key ? bidx : -1;
+        s_bkey = key;
+        if (!PK::kPacked) {
+          *reinterpret_cast<K*>(my + 8) = key;
+          *reinterpret_cast<int*>(my + 16) = key ? bidx : -1;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- 2. publish the candidate row and (owner) row c: the row's thread
+    // puts its registers into its sL row, then its warp copies the row out
+    const int tb = s_best >= 0 ? s_best - r0 : -1;
+    const int tc = (c >= r0 && c < r0 + nr) ? c - r0 : -1;
+    {
+      const bool wb = tb >= 0 && (tb >> 5) == warp;
+      const bool wc = tc >= 0 && (tc >> 5) == warp;
+      if (wb || wc) {
+        if (tid == tb || tid == tc) {
+#pragma unroll
+          for (int k = 0; k < NB; ++k) {
+            if (c + k >= w) break;
+            sL[tid * LD + c + k] = a[k];
+          }
+        }
+        __syncwarp();
+        V* rec = reinterpret_cast<V*>(my + kRecHeader);
+        if (wb)
+          for (int k = lane; k < w; k += 32) rec[k] = sL[tb * LD + k];
+        if (wc)
+          for (int k = lane; k < w; k += 32) rec[NB + k] = sL[tc * LD + k];
+      }
+    }
+    __syncthreads();
+    const unsigned tag = (unsigned)((j0 + c) & 127) + 1u;
+    if (tid == 0) {
+      __threadfence();
+      if (PK::kPacked)
+        st_release_u64(reinterpret_cast<unsigned long long*>(my), pack_flag(tag, s_best, (unsigned)s_bkey));
+      else
+        st_release_u64(reinterpret_cast<unsigned long long*>(my), seq0 + (unsigned long long)c);
+    }
+    // ---- 3. warp 0 waits for every CTA's flag and picks the global pivot
+    if (warp == 0) {
+      constexpr int kPer = (kMaxPanelBlocks + 31) / 32;
+      unsigned seen = 0;
+      const int per = (G + 31) / 32;
+      const unsigned want = (1u << per) - 1u;
+      unsigned it = 0;
+      bool ok = true;
+      K bk = 0;                 // this lane's best candidate so far
+      int bi = kNone;
+      while (true) {
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+          const int q = lane + 32 * j;
+          if (j >= per || (seen & (1u << j))) continue;
+          if (q >= G) { seen |= 1u << j; continue; }
+          const unsigned char* rq = ws.records + ((size_t)buf * kMaxPanelBlocks + q) * kRecBytes;
+          const unsigned long long f = ld_acquire_u64(reinterpret_cast<const unsigned long long*>(rq));
+          K k2;
+          int i2;
+          if (PK::kPacked) {
+            if ((unsigned)(f >> 56) != tag) continue;
+            k2 = (K)(unsigned)f;
+            i2 = (int)((f >> 32) & 0xFFFFFFu) - 1;
+          } else {
+            if (f != seq0 + (unsigned long long)c) continue;
+            k2 = __ldcg(reinterpret_cast<const K*>(rq + 8));
+            i2 = __ldcg(reinterpret_cast<const int*>(rq + 16));
+          }
+          seen |= 1u << j;
+          if (!k2) i2 = kNone;
+          if (k2 > bk || (k2 == bk && i2 < bi)) { bk = k2; bi = i2; }
+        }
+        if (__all_sync(0xffffffffu, seen == want)) break;
+        if (++it > kSpinLimit) { ok = false; break; }
+        if (it > 16) __nanosleep(20);
+      }
+      if (ok) warp_argmax(bk, bi);
+      if (lane == 0) {
+        s_p = bk ? bi : -1;
+        if (!ok) { s_fail = 1; atomicExch(ws.status, MGT_ERR_TIMEOUT); }
+      }
+    }
+    __syncthreads();
+    if (s_fail) return;
+    const int p = s_p >= 0 ? s_p : c;
+    const int wbk = s_p >= 0 ? s_p / rows_per_cta : -1;
+    const int owner = c / rows_per_cta;
+    // ---- 4. pivot row and row c from the records
+    if (tid < w) {
+      const V* rec_w = reinterpret_cast<const V*>(ws.records + ((size_t)buf * kMaxPanelBlocks + max(wbk, 0)) *
+                                                  kRecBytes + kRecHeader);
+      const V* rec_o = reinterpret_cast<const V*>(ws.records + ((size_t)buf * kMaxPanelBlocks + owner) *
+                                                  kRecBytes + kRecHeader) + NB;
+      const V rc = ldcg(rec_o + tid);
+      RC[tid] = rc;
+      U[tid] = wbk >= 0 ? ldcg(rec_w + tid) : rc;
+    }
+    __syncthreads();
+    const V piv = U[c];
+    const bool nz = (piv.x != 0 || piv.y != 0);
+    // ---- 5. interchange rows c and p: finished columns cooperatively, the rest in registers
+    if (nz && p != c) {
+      const int tp = (p >= r0 && p < r0 + nr) ? p - r0 : -1;
+      if (tid < c) {
+        if (tp >= 0) sL[tp * LD + tid] = RC[tid];
+        if (tc >= 0) sL[tc * LD + tid] = U[tid];
+      }
+      if (tid == tp || tid == tc) {
+        const V* src = tid == tp ? RC : U;
+#pragma unroll
+        for (int kc = 0; kc < NB; kc += kChunk) {
+          if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+          for (int k = kc; k < kc + kChunk; ++k) a[k] = src[c + k];
+        }
+      }
+    }
+    if (bid == 0 && tid == 0) {
+      s_piv[c] = nz ? p : c;
+      if (!nz && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
+    }
+    // ---- 6. scale and rank-1 update in registers, retire column c, shift
+    if (have && row > c && nz) {
+      const V l = cmul(a[0], crecip(piv));
+      a[0] = l;
+      // whole chunks of live columns; U is zero beyond w, so the tail of a chunk is a no-op
+#pragma unroll
+      for (int kc = 0; kc < NB; kc += kChunk) {
+        if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+        for (int k = (kc ? kc : 1); k < kc + kChunk; ++k) cfms(a[k], l, U[c + k]);
+      }
+    }
+    if (have) sL[tid * LD + c] = a[0];
+#pragma unroll
+    for (int kc = 0; kc < NB; kc += kChunk) {
+      if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+      for (int k = kc; k < kc + kChunk && k + 1 < NB; ++k) a[k] = a[k + 1];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < nr * NB; i += kPanelThreads) {
+    const int r = i / NB, k = i % NB;
+    if (k < w) A[(int64_t)(r0 + r) * lda + k] = sL[r * LD + k];
+  }
+
+  if (bid == 0 && warp == 0) {
+    for (int s2 = lane; s2 < NB; s2 += 32) { slot_pos[s2] = s2; slot_src[s2] = s2; }
+    if (lane == 0) s_nslot = NB;
+    __syncwarp();
+    for (int s2 = 0; s2 < w; ++s2) {
+      const int pv = s_piv[s2];
+      if (pv == s2) continue;
+      int slot = -1;
+      if (pv < NB) {
+        slot = pv;
+      } else {
+        const int ns = s_nslot;
+        for (int base = NB; base < ns && slot < 0; base += 32) {
+          int q = base + lane;
+          unsigned hit = __ballot_sync(0xffffffffu, q < ns && slot_pos[q] == pv);
+          if (hit) slot = base + __ffs(hit) - 1;
+        }
+        if (slot < 0) {
+          slot = ns;
+          if (lane == 0) { slot_pos[ns] = pv; slot_src[ns] = pv; s_nslot = ns + 1; }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) { int t2 = slot_src[s2]; slot_src[s2] = slot_src[slot]; slot_src[slot] = t2; }
+      __syncwarp();
+    }
+    const int ns = s_nslot;
+    for (int q = lane; q < ns; q += 32) ws.slots[q] = make_int2(slot_pos[q], slot_src[q]);
+    if (lane == 0) *ws.nslot = ns;
+    // the panel's interchanges applied to perm in one gather / scatter
+    int32_t pv[2 * NB / 32];
+#pragma unroll
+    for (int j = 0; j < 2 * NB / 32; ++j) {
+      const int q = lane + 32 * j;
+      if (q < ns) pv[j] = perm[j0 + slot_src[q]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 2 * NB / 32; ++j) {
+      const int q = lane + 32 * j;
+      if (q < ns) perm[j0 + slot_pos[q]] = pv[j];
+    }
+  }
+}
+
+constexpr size_t reg_panel_smem(int nb, size_t elem) { return (size_t)kPanelThreads * (nb + 1) * elem; }
+
 constexpr int kSwapCols = 32;
 
 // run-time tuning knobs (set by the autotuner; see mgt_set_tuning)
@@ -321,6 +637,7 @@ static std::atomic<int> g_panel_rows{kPanelRowsTarget};
 static std::atomic<int> g_outer_block{128};
 static std::atomic<int> g_panel_max_ctas{0};     // 0: one per SM
 static std::atomic<int> g_cooperative{1};        // panel launched with the cooperative attribute
+static std::atomic<int> g_panel_reg{1};          // register-resident panel: 0 never, 1 complex64, 2 both
 
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
@@ -439,11 +756,14 @@ lu_preupdate_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, in
   }
 }
 
-// perm = identity; the factorisation epoch moves on by one
-__global__ void lu_start_kernel(int32_t* perm, int n, unsigned long long* epoch) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// perm = identity; the factorisation epoch moves on by one; the panel records'
+// flags are cleared (the complex64 panel's short column tags rely on it)
+__global__ void lu_start_kernel(int32_t* perm, int n, unsigned long long* epoch, unsigned char* records) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) perm[i] = i;
   if (i == 0) *epoch += 1;
+  for (int r = i; r < 2 * kMaxPanelBlocks; r += gridDim.x * blockDim.x)
+    *reinterpret_cast<unsigned long long*>(records + (size_t)r * kRecBytes) = 0ull;
 }
 
 static int num_sms() {
@@ -484,10 +804,12 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     cudaFuncSetAttribute(lu_panel_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemBudget);
     cudaFuncSetAttribute(lu_swap_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
+    cudaFuncSetAttribute(lu_panel_reg_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)reg_panel_smem(NB, sizeof(V)));
   });
   PanelWs ws = panel_ws(work);
   if (cudaMemsetAsync(work, 0, 32, s) != cudaSuccess) return MGT_ERR_CUDA;   // status, nslot
-  lu_start_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n, ws.epoch);
+  lu_start_kernel<<<(n + 255) / 256, 256, 0, s>>>(perm, n, ws.epoch, ws.records);
   count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
   const size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
@@ -517,8 +839,16 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     // Without the attribute (CUDA-graph capture of concurrent branches) the
     // caller keeps the panels' total CTA count within the SM count instead.
     cfg.numAttrs = g_cooperative.load(std::memory_order_relaxed) ? 1 : 0;
-    if (cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws) != cudaSuccess)
-      return MGT_ERR_CUDA;
+    // up to one row per thread: the register-resident kernel
+    cudaError_t le;
+    const int reg_mode = g_panel_reg.load(std::memory_order_relaxed);
+    if (rpc <= kPanelThreads && (reg_mode == 2 || (reg_mode == 1 && sizeof(T) == 4))) {
+      cfg.dynamicSmemBytes = reg_panel_smem(NB, sizeof(V));
+      le = cudaLaunchKernelEx(&cfg, lu_panel_reg_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws);
+    } else {
+      le = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws);
+    }
+    if (le != cudaSuccess) return MGT_ERR_CUDA;
     count_launch();
     const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
     const int nright = (n - j0 - w + kSwapCols - 1) / kSwapCols;
@@ -858,6 +1188,11 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_cooperative.store(value ? 1 : 0);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_PANEL_REGISTERS) {
+    if (value < 0 || value > 2) return MGT_ERR_ARG;
+    g_panel_reg.store(value);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
@@ -866,5 +1201,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_OUTER_BLOCK) return g_outer_block.load();
   if (key == MGT_TUNE_PANEL_MAX_CTAS) return g_panel_max_ctas.load();
   if (key == MGT_TUNE_COOPERATIVE) return g_cooperative.load();
+  if (key == MGT_TUNE_PANEL_REGISTERS) return g_panel_reg.load();
   return MGT_ERR_ARG;
 }

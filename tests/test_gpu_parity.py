@@ -167,6 +167,43 @@ def test_lu_random(n, dtype):
     assert rel(Lm @ U, PA) < (1e-13 if dtype == torch.complex128 else 1e-4)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [torch.complex64, torch.complex128])
+@pytest.mark.parametrize("n,rows", [(700, 256), (3000, 64), (5000, 128)])
+def test_panel_kernels_agree(n, rows, dtype):
+    """The register-resident panel (one row per thread, integer pivot keys,
+    packed flags for complex64) and the shared-memory panel pick the same
+    pivots and produce bit-identical factors; many CTAs per panel at rows=64."""
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    lib = L.load()
+    gen = torch.Generator().manual_seed(n + rows)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen).to(dtype)
+    if n == 700:
+        A[5:40, 0] = 10 + 10j   # equal largest |re|+|im| in column 0: the lowest row (5) wins
+    outs = []
+    old_rows = lib.mgt_get_tuning(L.MGT_TUNE_PANEL_ROWS)
+    try:
+        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, rows)
+        for mode in (0, 2):
+            lib.mgt_set_tuning(L.MGT_TUNE_PANEL_REGISTERS, mode)
+            f = E.lu_factor(A.cuda().clone(), check_singular=False)
+            outs.append((f.lu.cpu(), f.perm.cpu()))
+    finally:
+        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_REGISTERS, 1)
+        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, old_rows)
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0], outs[1][0])
+    if n == 700:
+        assert int(outs[1][1][0]) == 5
+    # and the factors are right: P A = L U
+    LU = outs[1][0].to(torch.complex128)
+    Lm = torch.tril(LU, -1) + torch.eye(n, dtype=torch.complex128)
+    PA = A.to(torch.complex128)[outs[1][1].long()]
+    # complex64 factors of a random matrix: backward error grows like n * eps32
+    assert rel(Lm @ torch.triu(LU), PA) < (1e-13 if dtype == torch.complex128 else 5e-8 * n)
+
+
 def test_singular_matrix_raises():
     from magreete_gb300 import engine as E
     A = torch.randn(80, 80, dtype=torch.complex128)
