@@ -243,6 +243,11 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *   MGT_TUNE_PANEL_REGISTERS  panels with at most 256 rows per CTA keep one row
  *                        per thread in registers: 1 (default) for complex64,
  *                        2 for both types, 0 never (rows in shared memory)
+ *   MGT_TUNE_TC_PRECISION  split-product scheme of the complex64 tensor-core
+ *                        update: MGT_TC_F16X2 (default; operands scaled by
+ *                        powers of two, split into two fp16, kind::f16) or
+ *                        MGT_TC_TF32X3 (split into two tf32, kind::tf32); both
+ *                        give ~22 significant bits per operand
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -250,6 +255,9 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_PANEL_MAX_CTAS 3
 #define MGT_TUNE_COOPERATIVE 4
 #define MGT_TUNE_PANEL_REGISTERS 5
+#define MGT_TUNE_TC_PRECISION 6
+#define MGT_TC_TF32X3 0
+#define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);
 int mgt_get_tuning(int key);
 

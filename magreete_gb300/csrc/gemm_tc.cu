@@ -13,7 +13,16 @@
 // FP32 in TMEM as hi*hi + hi*lo + lo*hi ("TF32x3", the split-product scheme of
 // Markidis et al. 2018 / Ootomo & Yokota 2022), which keeps ~FP32 accuracy.
 //
-// Kernel: one CTA per 128 x 256 tile of C' (128 rows, 128 complex columns).
+// F16x2 variant (default): both operands are first scaled by a power of two
+// -- A per row, B per complex output column -- so that the largest magnitude
+// lies in [0.5, 1), then split x = hi + lo with hi = fp16(x), lo = fp16(x - hi)
+// (22 significant bits, the same as the TF32 split) and multiplied with
+// kind::f16 MMAs, which issue at twice the TF32 rate; the epilogue multiplies
+// the accumulator by the inverse scales.  Values below 2^-24 of their row's
+// (column's) largest flush to zero, an absolute error below that of FP32
+// rounding of the row's largest entry.
+//
+// Kernel: one CTA per 128 x 128 tile of C' (128 rows, 64 complex columns).
 //   warp 0 lane 0 : TMA producer (cp.async.bulk.tensor, 128B swizzle) of the
 //                   A_hi/A_lo (128 x 32 fp32) and B_hi/B_lo (256 x 32 fp32)
 //                   tiles of each 32-wide K block, 2-stage mbarrier ring
@@ -25,9 +34,11 @@
 // Every wait is bounded; on expiry the CTA records MGT_ERR_TIMEOUT, drains
 // the MMAs it issued, frees its TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -41,11 +52,10 @@ namespace tc {
 
 constexpr int BM = 128;            // tile rows (M)
 constexpr int BN = 128;            // tile real columns (N') = 64 complex columns
-constexpr int BK = 32;             // fp32 elements per 128-byte swizzle row
 constexpr int KR = 256;            // real K stride of the split buffers (2 * 128 complex)
 constexpr int STAGES = 2;
-constexpr uint32_t A_TILE = BM * BK * 4;   // 16 KB
-constexpr uint32_t B_TILE = BN * BK * 4;   // 16 KB
+constexpr uint32_t A_TILE = BM * 128;      // 16 KB: 128 rows of one 128-byte swizzle row
+constexpr uint32_t B_TILE = BN * 128;      // 16 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 64 KB
 constexpr int CHUNKS = BN / 32;            // epilogue chunks per tile (32 fp32 columns each)
 constexpr int CSLOTS = 4;                  // C chunk ring
@@ -109,14 +119,32 @@ __device__ __forceinline__ uint64_t kmajor_sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 256
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// Operand element per mode: K elements per 128-byte swizzle row (one stage)
+// and the instruction descriptor (D = F32, both operands K-major, M = 128,
+// N = 128): kind::tf32 with A = B = TF32 (code 2), kind::f16 with A = B = F16
+// (code 0).  Either way one MMA covers 32 bytes of K.
+template <bool F16>
+struct Mode {
+  static constexpr int ELEM = F16 ? 2 : 4;
+  static constexpr int BK = 128 / ELEM;
+  static constexpr uint32_t kAB = F16 ? 0u : 2u;
+  static constexpr uint32_t kIdesc =
+      (1u << 4) | (kAB << 7) | (kAB << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+};
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-      ::"r"(d_tmem), "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-      : "memory");
+template <bool F16>
+__device__ __forceinline__ void mma_split(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  if constexpr (F16) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(Mode<true>::kIdesc), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(Mode<false>::kIdesc), "r"(accumulate)
+        : "memory");
+  }
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -164,11 +192,15 @@ __device__ __forceinline__ bool epi_bar_and(bool p) {
 // holds two accumulators so the epilogue of tile t overlaps the MMAs of
 // tile t+1; C moves through a 4-slot ring of 128 x 32 fp32 chunks with TMA
 // loads (prefetched one tile ahead) and TMA stores.
+// invA / invB (F16 mode): inverse row scales of A and inverse complex-column
+// scales of B, relative to the block being updated.
+template <bool F16>
 __global__ void __launch_bounds__(THREADS, 1)
-cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
+cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                     const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
                     const __grid_constant__ CUtensorMap mapC, int cx0, int cy0, int tiles_n, int total_tiles,
-                    int kblocks, int* status) {
+                    int kblocks, const float* __restrict__ invA, const float* __restrict__ invB, int* status) {
+  constexpr int BK = Mode<F16>::BK;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* cring = base + STAGES * STAGE_BYTES;
@@ -237,11 +269,11 @@ cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
         const uint64_t ahi = kmajor_sw128_desc(st), alo = kmajor_sw128_desc(st + A_TILE);
         const uint64_t bhi = kmajor_sw128_desc(st + 2 * A_TILE), blo = kmajor_sw128_desc(st + 2 * A_TILE + B_TILE);
 #pragma unroll
-        for (int k = 0; k < BK / 8; ++k) {
-          const uint64_t off = (uint64_t)((k * 32) >> 4);   // 8 tf32 = 32 bytes along K
-          mma_tf32(d, alo + off, bhi + off, (kb | k) != 0);
-          mma_tf32(d, ahi + off, blo + off, 1);
-          mma_tf32(d, ahi + off, bhi + off, 1);
+        for (int k = 0; k < 4; ++k) {
+          const uint64_t off = (uint64_t)((k * 32) >> 4);   // 32 bytes along K per MMA
+          mma_split<F16>(d, alo + off, bhi + off, (kb | k) != 0);
+          mma_split<F16>(d, ahi + off, blo + off, 1);
+          mma_split<F16>(d, ahi + off, bhi + off, 1);
         }
         mma_commit(&empty[s]);
       }
@@ -273,10 +305,22 @@ cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
       if (!epi_bar_and(mbar_wait(&tfull[acc], (lt >> 1) & 1, abort))) break;
       tc_fence_after();
       bool ok = true;
+      const int tile = first + lt * stride;
+      const int tm0 = (tile / tiles_n) * BM, tn0 = (tile % tiles_n) * BN;
+      const float rs = F16 ? __ldg(invA + tm0 + r) : 1.f;
       for (int c = 0; c < CHUNKS; ++c) {
         const int g = lt * CHUNKS + c, slot = g % CSLOTS;
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c * 32), v);
+        if constexpr (F16) {
+          const float* cs = invB + ((tn0 + c * 32) >> 1);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float f = rs * __ldg(cs + j);
+            v[2 * j] *= f;
+            v[2 * j + 1] *= f;
+          }
+        }
         if (!epi_bar_and(mbar_wait(&cfull[slot], (g / CSLOTS) & 1, abort))) { ok = false; break; }
         unsigned char* rowp = cring + slot * CHUNK_BYTES + r * 128;
 #pragma unroll
@@ -383,6 +427,94 @@ __global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K,
   }
 }
 
+// F16 mode.  A (M x K complex) -> Ahi, Alo (fp16, M rows of stride KR): row i
+// scaled by 2^-e_i, e_i the exponent of its largest |re|, |im|
+// (max * 2^-e_i in [0.5, 1)); invA[i] = 2^e_i.  One warp per row.
+__global__ void split_a_f16_kernel(const float2* __restrict__ A, int64_t lda, int M, int K, int kcols,
+                                   __half* __restrict__ Ahi, __half* __restrict__ Alo, float* __restrict__ invA) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= M) return;
+  float v[KR / 32];
+  unsigned mx = 0;
+#pragma unroll
+  for (int j = 0; j < KR / 32; ++j) {
+    const int k = lane + 32 * j;
+    float x = 0.f;
+    if (k < 2 * K) {
+      const float2 a = A[(int64_t)i * lda + (k >> 1)];
+      x = (k & 1) ? a.y : a.x;
+    }
+    v[j] = x;
+    mx = max(mx, __float_as_uint(fabsf(x)));
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  int e = 0;
+  if (mx != 0u && mx < 0x7F800000u) {
+    frexpf(__uint_as_float(mx), &e);
+    e = max(-120, min(120, e));
+  }
+  const float sc = ldexpf(1.f, -e);
+#pragma unroll
+  for (int j = 0; j < KR / 32; ++j) {
+    const int k = lane + 32 * j;
+    if (k < kcols) {
+      const float x = v[j] * sc;
+      const __half h = __float2half_rn(x);
+      const int64_t o = (int64_t)i * KR + k;
+      Ahi[o] = h;
+      Alo[o] = __float2half_rn(x - __half2float(h));
+    }
+  }
+  if (lane == 0) invA[i] = ldexpf(1.f, e);
+}
+
+// F16 mode.  B (K x N complex) -> B'^T rows 2j, 2j+1 (fp16), both scaled by
+// 2^-e_j, e_j the exponent of the largest |re|, |im| of column j; invB[j] = 2^e_j.
+// Columns N .. (grid end) are zero (see split_b_kernel).
+__global__ void split_b_f16_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, int kcols,
+                                   __half* __restrict__ Bhi, __half* __restrict__ Blo, float* __restrict__ invB) {
+  __shared__ float2 t[128][33];
+  __shared__ float sc[32];
+  const int j0 = blockIdx.x * 32;
+  for (int idx = threadIdx.x; idx < 128 * 32; idx += blockDim.x) {
+    int k = idx / 32, jj = idx - k * 32;
+    t[k][jj] = (k < K && j0 + jj < N) ? B[(int64_t)k * ldb + j0 + jj] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  // column scales: warp w handles columns w, w + 8, ...
+  for (int jj = threadIdx.x >> 5; jj < 32; jj += blockDim.x >> 5) {
+    const int lane = threadIdx.x & 31;
+    unsigned mx = 0;
+    for (int k = lane; k < 128; k += 32)
+      mx = max(mx, max(__float_as_uint(fabsf(t[k][jj].x)), __float_as_uint(fabsf(t[k][jj].y))));
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    int e = 0;
+    if (mx != 0u && mx < 0x7F800000u) {
+      frexpf(__uint_as_float(mx), &e);
+      e = max(-120, min(120, e));
+    }
+    if (lane == 0) {
+      sc[jj] = ldexpf(1.f, -e);
+      invB[j0 + jj] = ldexpf(1.f, e);
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 64 * kcols; idx += blockDim.x) {
+    int r = idx / kcols, kr = idx - r * kcols;
+    int jj = r >> 1, j = j0 + jj;
+    int k = kr >> 1;
+    float2 b = t[k][jj];
+    float v;
+    if ((r & 1) == 0) v = (kr & 1) ? -b.y : b.x;
+    else v = (kr & 1) ? b.x : b.y;
+    v *= sc[jj];
+    const __half h = __float2half_rn(v);
+    int64_t o = (int64_t)(2 * j + (r & 1)) * KR + kr;
+    Bhi[o] = h;
+    Blo[o] = __float2half_rn(v - __half2float(h));
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -400,16 +532,17 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 2D fp32 tensor (rows x 128), box (32 x box_rows), 128-byte swizzle
-static bool make_map(CUtensorMap* map, float* base, int64_t rows, int box_rows) {
+// 2D tensor (rows x KR) of fp32 or fp16, box (one 128-byte row x box_rows), 128-byte swizzle
+static bool make_map(CUtensorMap* map, void* base, int64_t rows, int box_rows, bool f16) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
+  const int elem = f16 ? 2 : 4;
   cuuint64_t dims[2] = {(cuuint64_t)KR, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)KR * 4};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)KR * elem};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / elem), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  return fn(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -419,21 +552,37 @@ static bool make_map(CUtensorMap* map, float* base, int64_t rows, int box_rows) 
 static int64_t b_rows(int64_t n) { return 2 * n + tc::BN; }
 
 size_t tc_scratch_bytes(int64_t n) {
-  // Ahi, Alo: n x 128; Bhi, Blo: (2n + BN) x 128 (fp32)
-  return (size_t)(2 * n + 2 * b_rows(n)) * tc::KR * sizeof(float) + 4096;
+  // Ahi, Alo: n x KR; Bhi, Blo: (2n + BN) x KR (fp32 -- the larger mode), inverse scales, alignment
+  return (size_t)(2 * n + 2 * b_rows(n)) * tc::KR * sizeof(float) + (size_t)(n + b_rows(n)) * sizeof(float) + 4096;
 }
 
 bool tc_available() { return tc::encode_fn() != nullptr; }
 
+static std::atomic<int> g_tc_mode{MGT_TC_F16X2};
+
+int tc_set_mode(int mode) {
+  if (mode != MGT_TC_TF32X3 && mode != MGT_TC_F16X2) return MGT_ERR_ARG;
+  g_tc_mode.store(mode);
+  return MGT_OK;
+}
+int tc_get_mode() { return g_tc_mode.load(); }
+
+// Scratch: Ahi, Alo (nmax rows), Bhi, Blo (b_rows rows), KR elements a row
+// (fp32, or fp16 in F16 mode), then (F16) invA[nmax], invB[b_rows / 2].
 int TcPlan::init(void* scratch, int64_t nmax) {
+  mode = g_tc_mode.load();
+  const bool f16 = mode == MGT_TC_F16X2;
+  const size_t elem = f16 ? 2 : 4;
   char* b = (char*)(((uintptr_t)scratch + 1023) & ~(uintptr_t)1023);
-  Ahi = (float*)b;
-  Alo = Ahi + nmax * tc::KR;
-  Bhi = Alo + nmax * tc::KR;
-  Blo = Bhi + b_rows(nmax) * tc::KR;
+  Ahi = b;
+  Alo = b + (size_t)nmax * tc::KR * elem;
+  Bhi = (char*)Alo + (size_t)nmax * tc::KR * elem;
+  Blo = (char*)Bhi + (size_t)b_rows(nmax) * tc::KR * elem;
+  invA = (float*)((char*)Blo + (size_t)b_rows(nmax) * tc::KR * elem);
+  invB = invA + nmax;
   this->nmax = nmax;
-  bool ok = tc::make_map(&mAhi, Ahi, nmax, tc::BM) && tc::make_map(&mAlo, Alo, nmax, tc::BM) &&
-            tc::make_map(&mBhi, Bhi, b_rows(nmax), tc::BN) && tc::make_map(&mBlo, Blo, b_rows(nmax), tc::BN);
+  bool ok = tc::make_map(&mAhi, Ahi, nmax, tc::BM, f16) && tc::make_map(&mAlo, Alo, nmax, tc::BM, f16) &&
+            tc::make_map(&mBhi, Bhi, b_rows(nmax), tc::BN, f16) && tc::make_map(&mBlo, Blo, b_rows(nmax), tc::BN, f16);
   return ok ? MGT_OK : MGT_ERR_CUDA;
 }
 
@@ -470,22 +619,43 @@ int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K
   if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
   static std::once_flag once;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(tc::cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::SMEM_BYTES);
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::SMEM_BYTES);
   });
-  const int kblocks = (2 * K + tc::BK - 1) / tc::BK, kcols = kblocks * tc::BK;
-  int64_t na = (int64_t)M * kcols;
-  count_launch();
-  tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, kcols, plan.Ahi, plan.Alo);
-  count_launch();
+  const bool f16 = plan.mode == MGT_TC_F16X2;
+  const int bk = f16 ? tc::Mode<true>::BK : tc::Mode<false>::BK;
+  const int kblocks = (2 * K + bk - 1) / bk, kcols = kblocks * bk;
   // cover every column of the last tile (2N rounded up to BN reals)
-  tc::split_b_kernel<<<(int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32), 256, 0, s>>>(
-      B, ldb, K, N, kcols, plan.Bhi, plan.Blo);
+  const int bgrid = (int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32);
+  if (f16) {
+    count_launch();
+    tc::split_a_f16_kernel<<<(M + 7) / 8, 256, 0, s>>>(A, lda, M, K, kcols, (__half*)plan.Ahi, (__half*)plan.Alo,
+                                                       plan.invA);
+    count_launch();
+    tc::split_b_f16_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (__half*)plan.Bhi, (__half*)plan.Blo,
+                                                 plan.invB);
+  } else {
+    int64_t na = (int64_t)M * kcols;
+    count_launch();
+    tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, kcols, (float*)plan.Ahi,
+                                                                   (float*)plan.Alo);
+    count_launch();
+    tc::split_b_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (float*)plan.Bhi, (float*)plan.Blo);
+  }
   const int tiles_n = (2 * N + tc::BN - 1) / tc::BN, tiles_m = (M + tc::BM - 1) / tc::BM;
   const int total = tiles_n * tiles_m;
   int ctas = std::min(total, max_ctas > 0 ? max_ctas : tc_num_sms());
   count_launch();
-  tc::cgemm_tf32x3_kernel<<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap,
-                                                                   cx0, cy0, tiles_n, total, kblocks, status);
+  if (f16)
+    tc::cgemm_split3_kernel<true><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(
+        plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
+        status);
+  else
+    tc::cgemm_split3_kernel<false><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(
+        plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
+        status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 

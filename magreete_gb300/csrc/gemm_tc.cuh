@@ -9,16 +9,22 @@ namespace mgt {
 // Split operand buffers and their TMA descriptors, built once per
 // factorisation for matrices of order <= nmax.
 struct TcPlan {
-  float* Ahi = nullptr;
-  float* Alo = nullptr;
-  float* Bhi = nullptr;
-  float* Blo = nullptr;
+  void* Ahi = nullptr;     // fp32 (TF32x3) or fp16 (F16x2) split operands
+  void* Alo = nullptr;
+  void* Bhi = nullptr;
+  void* Blo = nullptr;
+  float* invA = nullptr;   // F16x2: inverse row scales of A, inverse column scales of B
+  float* invB = nullptr;
+  int mode = 0;            // MGT_TC_TF32X3 or MGT_TC_F16X2, fixed when the plan is built
   int64_t nmax = 0;
   CUtensorMap mAhi, mAlo, mBhi, mBlo;
   int init(void* scratch, int64_t nmax);
 };
 
 size_t tc_scratch_bytes(int64_t n);
+// split-product scheme of the tensor-core update (MGT_TC_TF32X3 / MGT_TC_F16X2)
+int tc_set_mode(int mode);
+int tc_get_mode();
 bool tc_available();
 
 // TMA map of a complex64 matrix C (rows x cols, leading dimension ldc even,

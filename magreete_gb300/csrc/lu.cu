@@ -1193,6 +1193,7 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_panel_reg.store(value);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_TC_PRECISION) return tc_set_mode(value);
   return MGT_ERR_ARG;
 }
 
@@ -1202,5 +1203,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_PANEL_MAX_CTAS) return g_panel_max_ctas.load();
   if (key == MGT_TUNE_COOPERATIVE) return g_cooperative.load();
   if (key == MGT_TUNE_PANEL_REGISTERS) return g_panel_reg.load();
+  if (key == MGT_TUNE_TC_PRECISION) return tc_get_mode();
   return MGT_ERR_ARG;
 }
