@@ -248,6 +248,10 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        powers of two, split into two fp16, kind::f16) or
  *                        MGT_TC_TF32X3 (split into two tf32, kind::tf32); both
  *                        give ~22 significant bits per operand
+ *   MGT_TUNE_LOOKAHEAD   1 (default): the complex64 tensor-core LU factors the
+ *                        next block's panels on a side stream's spare SMs while
+ *                        the rest of the trailing update runs (cooperative
+ *                        panels, not under stream capture); 0: strictly in order
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -256,6 +260,7 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_COOPERATIVE 4
 #define MGT_TUNE_PANEL_REGISTERS 5
 #define MGT_TUNE_TC_PRECISION 6
+#define MGT_TUNE_LOOKAHEAD 7
 #define MGT_TC_TF32X3 0
 #define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);

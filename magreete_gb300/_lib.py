@@ -28,6 +28,7 @@ MGT_NAN_KEEP, MGT_NAN_FILL = 0, 1
 MGT_TUNE_PANEL_ROWS, MGT_TUNE_OUTER_BLOCK, MGT_TUNE_PANEL_MAX_CTAS, MGT_TUNE_COOPERATIVE = 1, 2, 3, 4
 MGT_TUNE_PANEL_REGISTERS = 5
 MGT_TUNE_TC_PRECISION = 6
+MGT_TUNE_LOOKAHEAD = 7
 MGT_TC_TF32X3, MGT_TC_F16X2 = 0, 1
 
 _vp = ctypes.c_void_p

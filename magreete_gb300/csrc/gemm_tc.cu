@@ -613,10 +613,7 @@ static int tc_num_sms() {
   return sms;
 }
 
-int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
-                const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas) {
-  if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
-  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+static void tc_init_attrs() {
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc::cgemm_split3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -624,31 +621,55 @@ int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K
     cudaFuncSetAttribute(tc::cgemm_split3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)tc::SMEM_BYTES);
   });
-  const bool f16 = plan.mode == MGT_TC_F16X2;
-  const int bk = f16 ? tc::Mode<true>::BK : tc::Mode<false>::BK;
-  const int kblocks = (2 * K + bk - 1) / bk, kcols = kblocks * bk;
-  // cover every column of the last tile (2N rounded up to BN reals)
-  const int bgrid = (int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32);
-  if (f16) {
-    count_launch();
+}
+
+static int tc_kcols(const TcPlan& plan, int K) {
+  const int bk = plan.mode == MGT_TC_F16X2 ? tc::Mode<true>::BK : tc::Mode<false>::BK;
+  return ((2 * K + bk - 1) / bk) * bk;
+}
+
+int tc_split_a(const TcPlan& plan, int M, int K, const float2* A, int64_t lda, cudaStream_t s) {
+  if (M <= 0 || K <= 0) return MGT_OK;
+  if (K > 128 || M > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  const int kcols = tc_kcols(plan, K);
+  count_launch();
+  if (plan.mode == MGT_TC_F16X2) {
     tc::split_a_f16_kernel<<<(M + 7) / 8, 256, 0, s>>>(A, lda, M, K, kcols, (__half*)plan.Ahi, (__half*)plan.Alo,
                                                        plan.invA);
-    count_launch();
-    tc::split_b_f16_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (__half*)plan.Bhi, (__half*)plan.Blo,
-                                                 plan.invB);
   } else {
     int64_t na = (int64_t)M * kcols;
-    count_launch();
     tc::split_a_kernel<<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A, lda, M, K, kcols, (float*)plan.Ahi,
                                                                    (float*)plan.Alo);
-    count_launch();
-    tc::split_b_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (float*)plan.Bhi, (float*)plan.Blo);
   }
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+int tc_split_b(const TcPlan& plan, int N, int K, const float2* B, int64_t ldb, cudaStream_t s) {
+  if (N <= 0 || K <= 0) return MGT_OK;
+  if (K > 128 || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  const int kcols = tc_kcols(plan, K);
+  // cover every column of the last tile (2N rounded up to BN reals)
+  const int bgrid = (int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32);
+  count_launch();
+  if (plan.mode == MGT_TC_F16X2)
+    tc::split_b_f16_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (__half*)plan.Bhi, (__half*)plan.Blo,
+                                                 plan.invB);
+  else
+    tc::split_b_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (float*)plan.Bhi, (float*)plan.Blo);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, int cx0, int cy0, int* status,
+            cudaStream_t s, int max_ctas) {
+  if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
+  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  tc_init_attrs();
+  const int kblocks = tc_kcols(plan, K) / (plan.mode == MGT_TC_F16X2 ? tc::Mode<true>::BK : tc::Mode<false>::BK);
   const int tiles_n = (2 * N + tc::BN - 1) / tc::BN, tiles_m = (M + tc::BM - 1) / tc::BM;
   const int total = tiles_n * tiles_m;
   int ctas = std::min(total, max_ctas > 0 ? max_ctas : tc_num_sms());
   count_launch();
-  if (f16)
+  if (plan.mode == MGT_TC_F16X2)
     tc::cgemm_split3_kernel<true><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(
         plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
         status);
@@ -657,6 +678,16 @@ int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K
         plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
         status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
+                const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas) {
+  if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
+  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  int e = tc_split_a(plan, M, K, A, lda, s);
+  if (e == MGT_OK) e = tc_split_b(plan, N, K, B, ldb, s);
+  if (e == MGT_OK) e = tc_gemm(plan, cmap, M, N, K, cx0, cy0, status, s, max_ctas);
+  return e;
 }
 
 }  // namespace mgt

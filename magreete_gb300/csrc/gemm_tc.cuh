@@ -38,4 +38,11 @@ int tc_make_cmap(CUtensorMap* map, float2* C, int64_t rows, int64_t cols, int64_
 int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
                 const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas = 0);
 
+// The same in its three steps: operand splits into the plan's buffers, then
+// the tcgen05 kernel, which reads only the split buffers and the C block.
+int tc_split_a(const TcPlan& plan, int M, int K, const float2* A, int64_t lda, cudaStream_t s);
+int tc_split_b(const TcPlan& plan, int N, int K, const float2* B, int64_t ldb, cudaStream_t s);
+int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, int cx0, int cy0, int* status,
+            cudaStream_t s, int max_ctas = 0);
+
 }  // namespace mgt

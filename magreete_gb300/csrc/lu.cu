@@ -37,13 +37,13 @@ constexpr size_t kRecBytes = (kRecHeader + 2 * kNBmax * sizeof(double2) + 127) &
 // Workspace layout (byte offsets), identical for both element types.
 struct LuWsLayout {
   size_t status = 8;      // 2 x i32: error, info
-  size_t nslot = 16;      // i32: slots written by the last panel
+  size_t nslot = 16;      // 2 x i32: slots written by the last panel of each slot set
   size_t epoch = 40;      // u64: factorisation counter (bumped on the device, never cleared)
-  size_t slots = 64;      // 2*NBmax x int2 (pos, src)
+  size_t slots = 64;      // 2 sets x 2*NBmax x int2 (pos, src)
   size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
   size_t total;
   LuWsLayout() {
-    records = (slots + 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
+    records = (slots + 2 * 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
     total = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
   }
 };
@@ -56,14 +56,15 @@ struct PanelWs {
   unsigned char* records;
 };
 
-static PanelWs panel_ws(void* work) {
+// slot set 0 or 1: two panels' interchanges can be pending at once (lookahead)
+static PanelWs panel_ws(void* work, int set = 0) {
   LuWsLayout L;
   char* b = (char*)work;
   PanelWs w;
   w.status = (int*)(b + L.status);
-  w.nslot = (int*)(b + L.nslot);
+  w.nslot = (int*)(b + L.nslot) + set;
   w.epoch = (unsigned long long*)(b + L.epoch);
-  w.slots = (int2*)(b + L.slots);
+  w.slots = (int2*)(b + L.slots) + set * 2 * kNBmax;
   w.records = (unsigned char*)(b + L.records);
   return w;
 }
@@ -638,22 +639,25 @@ static std::atomic<int> g_outer_block{128};
 static std::atomic<int> g_panel_max_ctas{0};     // 0: one per SM
 static std::atomic<int> g_cooperative{1};        // panel launched with the cooperative attribute
 static std::atomic<int> g_panel_reg{1};          // register-resident panel: 0 never, 1 complex64, 2 both
+static std::atomic<int> g_lookahead{1};          // tensor-core LU: next block's panels beside the update
 
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
 template <typename T, int NB>
 __global__ void __launch_bounds__(256)
-lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int nleft_blocks,
-                    PanelWs ws, int do_trsm = 1) {
+lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int left_end, int right_begin,
+                    int right_end, PanelWs ws, int do_trsm) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* buf = reinterpret_cast<V*>(smem_raw);   // [2*NB][kSwapCols]
   V* L = buf + 2 * NB * kSwapCols;            // [NB][NB]
   const int tid = threadIdx.x;
-  const bool right_cols = blockIdx.x >= nleft_blocks;
+  // columns [0, left_end) left of the panel, [right_begin, right_end) right of it
+  const int nleft_blocks = (left_end + kSwapCols - 1) / kSwapCols;
+  const bool right_cols = (int)blockIdx.x >= nleft_blocks;
   const bool right = right_cols && do_trsm;   // columns right of the panel that get the solve
-  const int col0 = right_cols ? j0 + w + (blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
-  const int colend = right_cols ? n : j0;
+  const int col0 = right_cols ? right_begin + ((int)blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
+  const int colend = right_cols ? right_end : left_end;
   const int ncols = min(kSwapCols, colend - col0);
   const int m = n - j0;
   const int ns = min(*ws.nslot, 2 * NB);
@@ -785,14 +789,34 @@ struct TcLU {
   CUtensorMap cmap;   // the whole matrix being factored
 };
 static int trailing_update(const TcLU* tc, int M, int N, int K, const double2* A, int64_t lda, const double2* B,
-                           int64_t ldb, double2* C, int64_t ldc, int, int*, cudaStream_t s) {
+                           int64_t ldb, double2* C, int64_t ldc, int, int*, cudaStream_t s, int) {
   (void)tc;
   return gemm_sub<double>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
 static int trailing_update(const TcLU* tc, int M, int N, int K, const float2* A, int64_t lda, const float2* B,
-                           int64_t ldb, float2* C, int64_t ldc, int c0, int* status, cudaStream_t s) {
-  if (tc) return gemm_sub_tc(tc->plan, tc->cmap, M, N, K, A, lda, B, ldb, 2 * c0, c0, status, s);
+                           int64_t ldb, float2* C, int64_t ldc, int c0, int* status, cudaStream_t s, int max_ctas) {
+  if (tc) return gemm_sub_tc(tc->plan, tc->cmap, M, N, K, A, lda, B, ldb, 2 * c0, c0, status, s, max_ctas);
   return gemm_sub<float>(M, N, K, A, lda, B, ldb, C, ldc, s);
+}
+
+// Per-thread side stream and fork / join events for the lookahead update.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int device = -1;
+};
+static SideStream* side_stream() {
+  thread_local SideStream ss;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (ss.device != dev) {
+    if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess)
+      return nullptr;
+    ss.device = dev;
+  }
+  return &ss;
 }
 
 template <typename T, int NB>
@@ -813,19 +837,22 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   count_launch();
   const int sms = std::min(num_sms(), kMaxPanelBlocks);
   const size_t sm2 = (2 * NB * kSwapCols + NB * NB) * sizeof(V);
-  // one inner panel: factor columns [j0, j0+w) over rows [j0, n), then apply
-  // its interchanges to every other column (and, when do_trsm, solve L11 U12 = A12
-  // for the columns right of the panel)
-  auto panel_step = [&](int j0, int w, int do_trsm) -> int {
-    const int m = n - j0;
+  // CTAs of the panel kernel for a panel of m rows
+  auto panel_ctas = [&](int m) -> int {
     const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
     const int rows_target = g_panel_rows.load(std::memory_order_relaxed);
     int G = (int)std::max<int64_t>({1, (m + rows_target - 1) / rows_target, min_g_smem});
     const int gmax = g_panel_max_ctas.load(std::memory_order_relaxed);
-    G = std::min(G, gmax > 0 ? std::min(gmax, sms) : sms);
+    return std::min(G, gmax > 0 ? std::min(gmax, sms) : sms);
+  };
+  // factor columns [j0, j0+w) over rows [j0, n); the interchanges go to slot set `set`
+  auto panel_only = [&](int j0, int w, int set) -> int {
+    const int m = n - j0;
+    const int G = panel_ctas(m);
     int rpc = (m + G - 1) / G;
     size_t smem = (size_t)rpc * NB * sizeof(V);
     if (smem > kPanelSmemBudget) return MGT_ERR_UNSUPPORTED;
+    PanelWs pw = panel_ws(work, set);
     V* P = A + (int64_t)j0 * lda + j0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(G);
@@ -844,36 +871,53 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int reg_mode = g_panel_reg.load(std::memory_order_relaxed);
     if (rpc <= kPanelThreads && (reg_mode == 2 || (reg_mode == 1 && sizeof(T) == 4))) {
       cfg.dynamicSmemBytes = reg_panel_smem(NB, sizeof(V));
-      le = cudaLaunchKernelEx(&cfg, lu_panel_reg_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws);
+      le = cudaLaunchKernelEx(&cfg, lu_panel_reg_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, pw);
     } else {
-      le = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, ws);
+      le = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, pw);
     }
     if (le != cudaSuccess) return MGT_ERR_CUDA;
     count_launch();
-    const int nleft = (j0 + kSwapCols - 1) / kSwapCols;
-    const int nright = (n - j0 - w + kSwapCols - 1) / kSwapCols;
-    if (nleft + nright > 0) {
-      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, s>>>(A, lda, n, j0, w, nleft, ws, do_trsm);
-      count_launch();
-    }
     return MGT_OK;
   };
-  auto update = [&](int r0, int c0, int k0, int K, int rows, int cols, bool dominant) -> int {
+  // apply the interchanges of the panel at j0 (slot set `set`) to columns
+  // [0, left_end) and [right_begin, right_end); with do_trsm the latter also get
+  // U12 = L11^-1 A12 on the panel's rows
+  auto swap = [&](cudaStream_t st, int j0, int w, int set, int left_end, int right_begin, int right_end,
+                  int do_trsm) {
+    const int nleft = (left_end + kSwapCols - 1) / kSwapCols;
+    const int nright = right_end > right_begin ? (right_end - right_begin + kSwapCols - 1) / kSwapCols : 0;
+    if (nleft + nright > 0) {
+      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, st>>>(A, lda, n, j0, w, left_end, right_begin,
+                                                                    right_end, panel_ws(work, set), do_trsm);
+      count_launch();
+    }
+  };
+  // one inner panel, then its interchanges on every other column
+  auto panel_step = [&](int j0, int w, int do_trsm) -> int {
+    int e = panel_only(j0, w, 0);
+    if (e == MGT_OK) swap(s, j0, w, 0, j0, j0 + w, n, do_trsm);
+    return e;
+  };
+  auto update_on = [&](cudaStream_t st, int r0, int c0, int k0, int K, int rows, int cols, bool dominant,
+                       int max_ctas) -> int {
     // A[r0:r0+rows, c0:c0+cols] -= A[r0:, k0:k0+K] * A[k0:k0+K, c0:]
     if (rows <= 0 || cols <= 0) return MGT_OK;
-    if (dominant) dom_begin(s);
+    if (dominant) dom_begin(st);
     int e;
     if (dominant)
       e = trailing_update(tc, rows, cols, K, A + (int64_t)r0 * lda + k0, lda, A + (int64_t)k0 * lda + c0, lda,
-                          A + (int64_t)r0 * lda + c0, lda, c0, ws.status, s);
+                          A + (int64_t)r0 * lda + c0, lda, c0, ws.status, st, max_ctas);
     else
       e = gemm_sub<T>(rows, cols, K, A + (int64_t)r0 * lda + k0, lda, A + (int64_t)k0 * lda + c0, lda,
-                      A + (int64_t)r0 * lda + c0, lda, s);
+                      A + (int64_t)r0 * lda + c0, lda, st);
     // algorithmic work of C -= A B: 8 rows cols K real flops; C read + written once, A and B read once
     if (dominant)
-      dom_end(s, 8.0 * rows * (double)cols * K,
+      dom_end(st, 8.0 * rows * (double)cols * K,
               sizeof(V) * (2.0 * rows * (double)cols + (double)rows * K + (double)K * cols));
     return e;
+  };
+  auto update = [&](int r0, int c0, int k0, int K, int rows, int cols, bool dominant) -> int {
+    return update_on(s, r0, c0, k0, K, rows, cols, dominant, 0);
   };
   if (tc == nullptr || g_outer_block.load(std::memory_order_relaxed) == NB) {
     for (int j0 = 0; j0 < n; j0 += NB) {
@@ -891,24 +935,110 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   std::call_once(once2, [sm3] {
     cudaFuncSetAttribute(lu_preupdate_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   });
-  for (int J0 = 0; J0 < n; J0 += 2 * NB) {
+  // Lookahead (cooperative panels, not under stream capture): the trailing
+  // update of block J0 first brings the next block's columns up to date, then
+  // the rest of it runs on a side stream with its CTAs capped to leave the
+  // next panels their SMs, while this stream factors the next block's two
+  // inner panels and applies their interchanges to the columns the side
+  // stream does not touch.  The far-right interchanges, the second panel's
+  // pre-update and the U12 solve follow once the side stream has finished.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
+  SideStream* side = nullptr;
+  if (g_lookahead.load(std::memory_order_relaxed) && g_cooperative.load(std::memory_order_relaxed) &&
+      cap == cudaStreamCaptureStatusNone)
+    side = side_stream();
+  // the two inner panels of the block at J0 and everything up to (not
+  // including) the columns at or right of `far`: interchanges on the left,
+  // the second panel's columns brought up to date
+  auto block_panels = [&](int J0, int far) -> int {
     const int W = std::min(2 * NB, n - J0), wa = std::min(NB, W), wb = W - wa, j1 = J0 + wa;
-    int e = panel_step(J0, wa, 1);
+    int e = panel_only(J0, wa, 0);
     if (e != MGT_OK) return e;
+    swap(s, J0, wa, 0, J0, j1, std::min(far, J0 + W), 1);
     if (wb > 0) {
-      // bring the second inner panel's columns up to date, factor it
       e = update(j1, j1, J0, wa, n - j1, wb, false);
-      if (e == MGT_OK) e = panel_step(j1, wb, 0);
+      if (e == MGT_OK) e = panel_only(j1, wb, 1);
       if (e != MGT_OK) return e;
-      const int right = n - J0 - W;
-      if (right > 0) {
-        lu_preupdate_trsm_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, sm3, s>>>(A, lda, n, J0, wa, j1,
-                                                                                             wb, J0 + W);
-        count_launch();
-      }
+      swap(s, j1, wb, 1, j1, 0, 0, 0);
     }
-    e = update(J0 + W, J0 + W, J0, W, n - J0 - W, n - J0 - W, true);
+    return MGT_OK;
+  };
+  // the far-right columns [J0 + W, n) of the block at J0: both panels'
+  // interchanges, the first panel's solve, the second panel's pre-update + solve
+  auto block_right = [&](int J0) {
+    const int W = std::min(2 * NB, n - J0), wa = std::min(NB, W), wb = W - wa, j1 = J0 + wa;
+    const int right = n - J0 - W;
+    if (right <= 0) return;
+    swap(s, J0, wa, 0, 0, J0 + W, n, 1);
+    if (wb > 0) {
+      swap(s, j1, wb, 1, 0, J0 + W, n, 0);
+      lu_preupdate_trsm_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, sm3, s>>>(A, lda, n, J0, wa, j1,
+                                                                                           wb, J0 + W);
+      count_launch();
+    }
+  };
+  auto lookahead_update = [&](int J0, int W, int P0, int WN, int rest, cudaStream_t s2) -> int {
+    if constexpr (sizeof(T) == 4) {
+      const int M = n - P0;
+      const float2* L21 = reinterpret_cast<const float2*>(A + (int64_t)P0 * lda + J0);
+      const float2* U12 = reinterpret_cast<const float2*>(A + (int64_t)J0 * lda + P0);
+      dom_begin(s);
+      int e = tc_split_a(tc->plan, M, W, L21, lda, s);
+      if (e == MGT_OK) e = tc_split_b(tc->plan, WN, W, U12, lda, s);
+      if (e == MGT_OK) e = tc_gemm(tc->plan, tc->cmap, M, WN, W, 2 * P0, P0, ws.status, s);
+      dom_end(s, 8.0 * M * (double)WN * W, sizeof(V) * (2.0 * M * (double)WN + (double)M * W + (double)W * WN));
+      if (e == MGT_OK) e = tc_split_b(tc->plan, rest, W, U12 + WN, lda, s);
+      if (e != MGT_OK) return e;
+      if (cudaEventRecord(side->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, side->fork, 0) != cudaSuccess)
+        return MGT_ERR_CUDA;
+      dom_begin(s2);
+      e = tc_gemm(tc->plan, tc->cmap, M, rest, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - panel_ctas(M)));
+      dom_end(s2, 8.0 * M * (double)rest * W, sizeof(V) * (2.0 * M * (double)rest + (double)W * rest));
+      // once forked, the join is recorded whatever happened
+      const bool joined = cudaEventRecord(side->join, s2) == cudaSuccess;
+      return e != MGT_OK ? e : (joined ? MGT_OK : MGT_ERR_CUDA);
+    } else {
+      (void)J0; (void)W; (void)P0; (void)WN; (void)rest; (void)s2;
+      return MGT_ERR_UNSUPPORTED;
+    }
+  };
+  if constexpr (sizeof(T) != 4) side = nullptr;   // the tensor-core path is complex64 only
+  int e = block_panels(0, n);
+  if (e != MGT_OK) return e;
+  block_right(0);
+  for (int J0 = 0; J0 < n; J0 += 2 * NB) {
+    const int W = std::min(2 * NB, n - J0);
+    const int P0 = J0 + W;                       // next block
+    if (P0 >= n) break;
+    const int WN = std::min(2 * NB, n - P0);
+    const int rest = n - P0 - WN;
+    // overlap only where it pays: the side update runs on the SMs the next
+    // panels leave free (estimates: update at ~250 TF/s on the full GPU, two
+    // inner panels at ~4.5 us per column plus their interchanges)
+    bool overlap = side != nullptr && rest > 0;
+    if (overlap) {
+      const int G = panel_ctas(n - P0);
+      const double t_upd = 8.0 * (n - P0) * (double)rest * W / 2.5e14;
+      const double t_pan = 2.0 * NB * 4.5e-6 + 1e-4;
+      overlap = sms - G >= 16 && std::max(t_upd * sms / (sms - G), t_pan) < t_upd + t_pan;
+    }
+    if (!overlap) {
+      e = update(P0, P0, J0, W, n - P0, n - P0, true);
+      if (e == MGT_OK) e = block_panels(P0, n);
+      if (e != MGT_OK) return e;
+      block_right(P0);
+      continue;
+    }
+    // A[P0:, P0:] -= L21 U12 of block J0: the operand splits (the rows of L21
+    // are permuted by the next panels' interchanges) and the next block's
+    // columns here; the rest of the update on the side stream
+    e = lookahead_update(J0, W, P0, WN, rest, side->s);
+    if (e == MGT_OK) e = block_panels(P0, P0 + WN);
+    // always join: nothing of the side stream may outlive this call
+    if (cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess && e == MGT_OK) e = MGT_ERR_CUDA;
     if (e != MGT_OK) return e;
+    block_right(P0);
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
@@ -1194,6 +1324,10 @@ extern "C" int mgt_set_tuning(int key, int value) {
     return MGT_OK;
   }
   if (key == MGT_TUNE_TC_PRECISION) return tc_set_mode(value);
+  if (key == MGT_TUNE_LOOKAHEAD) {
+    g_lookahead.store(value ? 1 : 0);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
@@ -1204,5 +1338,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_COOPERATIVE) return g_cooperative.load();
   if (key == MGT_TUNE_PANEL_REGISTERS) return g_panel_reg.load();
   if (key == MGT_TUNE_TC_PRECISION) return tc_get_mode();
+  if (key == MGT_TUNE_LOOKAHEAD) return g_lookahead.load();
   return MGT_ERR_ARG;
 }

@@ -204,6 +204,29 @@ def test_panel_kernels_agree(n, rows, dtype):
     assert rel(Lm @ torch.triu(LU), PA) < (1e-13 if dtype == torch.complex128 else 5e-8 * n)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [700, 5000, 9000])
+def test_lookahead_matches_in_order(n):
+    """The complex64 tensor-core LU with the next block's panels overlapped on a
+    side stream gives bit-identical factors and pivots to the in-order one."""
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    lib = L.load()
+    gen = torch.Generator().manual_seed(n + 17)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen).to(torch.complex64)
+    outs = []
+    try:
+        for mode in (0, 1):
+            lib.mgt_set_tuning(L.MGT_TUNE_LOOKAHEAD, mode)
+            f = E.lu_factor(A.cuda().clone(), check_singular=False)
+            torch.cuda.synchronize()
+            outs.append((f.lu.cpu(), f.perm.cpu()))
+    finally:
+        lib.mgt_set_tuning(L.MGT_TUNE_LOOKAHEAD, 1)
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[0][0], outs[1][0])
+
+
 def test_singular_matrix_raises():
     from magreete_gb300 import engine as E
     A = torch.randn(80, 80, dtype=torch.complex128)
