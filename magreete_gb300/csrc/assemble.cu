@@ -86,7 +86,7 @@ template <int KIND, bool TRANSPOSE>
 __global__ void __launch_bounds__(kAsmThreads)
 assemble_propagator_kernel(const double* __restrict__ tgt, int nt, const double* __restrict__ src,
                            int ns, double k0, double2 coef, bool regularize, double radius,
-                           int nan_policy, double2 fill, double2* __restrict__ out, int64_t ld) {
+                           int nan_policy, double2 fill, OutSpec out) {
   constexpr int dim = Kind<KIND>::dim, d = Kind<KIND>::d;
   int ncol = TRANSPOSE ? nt : ns, nrow = TRANSPOSE ? ns : nt;
   int q = blockIdx.x * kAsmThreads + threadIdx.x;
@@ -123,9 +123,9 @@ assemble_propagator_kernel(const double* __restrict__ tgt, int nt, const double*
 #pragma unroll
     for (int a = 0; a < d; ++a) {
       // output row index d*p + a; block entry G_ab (normal) or G_ba (transposed)
-      double2* o = out + ((int64_t)p * d + a) * ld + (int64_t)q * d;
 #pragma unroll
-      for (int b = 0; b < d; ++b) o[b] = TRANSPOSE ? g[b * d + a] : g[a * d + b];
+      for (int b = 0; b < d; ++b)
+        store_entry(out, (int64_t)p * d + a, (int64_t)q * d + b, TRANSPOSE ? g[b * d + a] : g[a * d + b]);
     }
   }
 }
@@ -142,15 +142,32 @@ static cudaError_t launch_system(const double* pts, int n, double k0, double2 co
 template <int KIND>
 static cudaError_t launch_prop(const double* t, int nt, const double* src, int ns, double k0,
                                double2 coef, bool reg, double radius, int nanp, double2 fill,
-                               int transpose, double2* out, int64_t ld, cudaStream_t s) {
+                               int transpose, OutSpec out, cudaStream_t s) {
   int ncol = transpose ? nt : ns, nrow = transpose ? ns : nt;
   dim3 grid((ncol + kAsmThreads - 1) / kAsmThreads, (nrow + kAsmRows - 1) / kAsmRows);
   count_launch();
   if (transpose)
-    assemble_propagator_kernel<KIND, true><<<grid, kAsmThreads, 0, s>>>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, out, ld);
+    assemble_propagator_kernel<KIND, true><<<grid, kAsmThreads, 0, s>>>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, out);
   else
-    assemble_propagator_kernel<KIND, false><<<grid, kAsmThreads, 0, s>>>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, out, ld);
+    assemble_propagator_kernel<KIND, false><<<grid, kAsmThreads, 0, s>>>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, out);
   return cudaGetLastError();
+}
+
+// Propagator blocks into any output format (used by the propagation's
+// assembled double-float path).
+int assemble_propagator_into(int kind, const double* t, int nt, const double* src, int ns, double k0, double2 coef,
+                             bool reg, double radius, int nanp, double2 fill, int transpose, void* out, int64_t ld,
+                             int dtype, cudaStream_t s) {
+  if (((transpose ? ns : nt) + kAsmRows - 1) / kAsmRows > 65535) return MGT_ERR_UNSUPPORTED;
+  OutSpec o{out, ld, dtype};
+  cudaError_t e;
+  switch (kind) {
+    case MGT_2D_VECTOR: e = launch_prop<MGT_2D_VECTOR>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, transpose, o, s); break;
+    case MGT_2D_SCALAR: e = launch_prop<MGT_2D_SCALAR>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, transpose, o, s); break;
+    case MGT_3D_VECTOR: e = launch_prop<MGT_3D_VECTOR>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, transpose, o, s); break;
+    default: e = launch_prop<MGT_3D_SCALAR>(t, nt, src, ns, k0, coef, reg, radius, nanp, fill, transpose, o, s); break;
+  }
+  return e == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
 }  // namespace mgt
@@ -201,18 +218,8 @@ extern "C" int mgt_assemble_propagator(int kind, const double* targets, int64_t 
   if (nan_policy != MGT_NAN_KEEP && nan_policy != MGT_NAN_FILL) return MGT_ERR_ARG;
   int64_t ncols = transpose ? d * n_targets : d * n_sources;
   if (ld < ncols) return MGT_ERR_ARG;
-  if (((transpose ? n_sources : n_targets) + kAsmRows - 1) / kAsmRows > 65535) return MGT_ERR_UNSUPPORTED;
   cudaStream_t s = (cudaStream_t)stream;
   double2 coef = make_double2(coef_re, coef_im), fill = make_double2(fill_re, fill_im);
-  int nt = (int)n_targets, ns = (int)n_sources;
-  bool reg = regularize != 0;
-  double2* o = (double2*)out_c128;
-  cudaError_t e;
-  switch (kind) {
-    case MGT_2D_VECTOR: e = launch_prop<MGT_2D_VECTOR>(targets, nt, sources, ns, k0, coef, reg, radius, nan_policy, fill, transpose, o, ld, s); break;
-    case MGT_2D_SCALAR: e = launch_prop<MGT_2D_SCALAR>(targets, nt, sources, ns, k0, coef, reg, radius, nan_policy, fill, transpose, o, ld, s); break;
-    case MGT_3D_VECTOR: e = launch_prop<MGT_3D_VECTOR>(targets, nt, sources, ns, k0, coef, reg, radius, nan_policy, fill, transpose, o, ld, s); break;
-    default: e = launch_prop<MGT_3D_SCALAR>(targets, nt, sources, ns, k0, coef, reg, radius, nan_policy, fill, transpose, o, ld, s); break;
-  }
-  return e == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+  return assemble_propagator_into(kind, targets, (int)n_targets, sources, (int)n_sources, k0, coef, regularize != 0,
+                                  radius, nan_policy, fill, transpose, out_c128, ld, MGT_C128, s);
 }

@@ -7,10 +7,13 @@
 // Here each CTA owns 16 detectors and all (up to 64) right-hand-side
 // columns of one source range: it evaluates the 16 x 8 Green's blocks of a
 // source chunk in FP64 into shared memory, stages the matching Ek rows, and
-// contracts.  The contraction runs in FP64 (plain method) or double-float on
-// the FP32 pipes (fast method).  Source ranges are split across CTAs for
-// parallelism; a second kernel sums the partials in FP64 and applies coef
-// and E0.
+// contracts in FP64.  Source ranges are split across CTAs for parallelism; a
+// second kernel sums the partials in FP64 and applies coef and E0.  That is
+// the plain method.  The fast method (MGT_CDF) assembles the propagator rows
+// in FP64 once, stored double-float, and contracts them with the residual
+// kernel in double-float on the FP32 pipes: each Green's block is evaluated
+// once for all right-hand sides, and the FP64 evaluation no longer stalls the
+// contraction.
 #include <algorithm>
 #include <mutex>
 #include <type_traits>
@@ -200,6 +203,38 @@ static void launch_partial_kind(int kind, int rt, dim3 grid, const double* t, in
   }
 }
 
+int assemble_propagator_into(int kind, const double* t, int nt, const double* src, int ns, double k0, double2 coef,
+                             bool reg, double radius, int nanp, double2 fill, int transpose, void* out, int64_t ld,
+                             int dtype, cudaStream_t s);
+int residual_rect(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B, int64_t ldb,
+                  double2* R, int64_t ldr, int rows, int kdim, int nrhs, cudaStream_t s, double2* partial,
+                  int64_t partial_elems);
+int residual_ksplit(int rows, int kdim);
+int split_df(const double2* X, int64_t ldx, float4* Xs, int64_t ldy, int n, int ncols, cudaStream_t s);
+
+// Double-float path: the propagator's detector rows are assembled in chunks
+// of at most kPropChunkBytes (as -coef G, double-float) and contracted with
+// the double-float copy of Ek by the residual kernel: out = E0 - (-coef G) Ek.
+constexpr size_t kPropChunkBytes = size_t(1) << 30;
+static int64_t prop_chunk_targets(int64_t nt, int64_t ns, int d) {
+  const int64_t row_bytes = (int64_t)d * d * ns * (int64_t)sizeof(float4);   // one target's d rows
+  return std::max<int64_t>(1, std::min<int64_t>(nt, (int64_t)kPropChunkBytes / std::max<int64_t>(1, row_bytes)));
+}
+// workspace: Xs (d ns x nrhs float4) | one chunk of propagator rows | split-K partials
+static size_t prop_xs_bytes(int64_t ns, int64_t nrhs, int d) {
+  return ((size_t)d * ns * nrhs * sizeof(float4) + 255) & ~size_t(255);
+}
+static size_t prop_chunk_bytes(int64_t nt, int64_t ns, int d) {
+  return ((size_t)prop_chunk_targets(nt, ns, d) * d * d * ns * sizeof(float4) + 255) & ~size_t(255);
+}
+static size_t prop_part_elems(int64_t nt, int64_t ns, int64_t nrhs, int d) {
+  const int64_t ct = prop_chunk_targets(nt, ns, d);
+  return (size_t)residual_ksplit((int)(ct * d), (int)(d * ns)) * ct * d * std::min<int64_t>(nrhs, 128);
+}
+static size_t prop_df_bytes(int64_t nt, int64_t ns, int64_t nrhs, int d) {
+  return prop_xs_bytes(ns, nrhs, d) + prop_chunk_bytes(nt, ns, d) + prop_part_elems(nt, ns, nrhs, d) * sizeof(double2);
+}
+
 static int kind_dim_d(int kind, int* dim) {
   switch (kind) {
     case MGT_2D_VECTOR: *dim = 2; return 2;
@@ -220,7 +255,10 @@ extern "C" int mgt_propagate_workspace_bytes(int kind, int64_t n_targets, int64_
   int d = kind_dim_d(kind, &dim);
   if (!bytes || d == 0 || n_targets <= 0 || n_sources <= 0 || nrhs <= 0) return MGT_ERR_ARG;
   int nsplit = choose_splits(n_targets, n_sources);
-  *bytes = (size_t)nsplit * n_targets * d * std::min<int64_t>(nrhs, kPCols) * sizeof(double2);
+  // the larger of the two methods' needs: FP64 partial sums, or the
+  // double-float copy of Ek plus one chunk of assembled propagator rows
+  *bytes = std::max((size_t)nsplit * n_targets * d * std::min<int64_t>(nrhs, kPCols) * sizeof(double2),
+                    prop_df_bytes(n_targets, n_sources, nrhs, d));
   return MGT_OK;
 }
 
@@ -240,6 +278,25 @@ extern "C" int mgt_propagate(int kind, int dtype, const double* targets, int64_t
   if (work_bytes < need) return MGT_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   const int nt = (int)n_targets, ns = (int)n_sources;
+  if (dtype == MGT_CDF) {
+    const int64_t ct = prop_chunk_targets(nt, ns, d);
+    float4* Xs = (float4*)work;
+    float4* Gc = (float4*)((char*)work + prop_xs_bytes(ns, nrhs, d));
+    double2* part = (double2*)((char*)Gc + prop_chunk_bytes(nt, ns, d));
+    int e = split_df((const double2*)Ek, ld_ek, Xs, nrhs, d * ns, (int)nrhs, st);
+    const double2 mcoef = make_double2(-coef_re, -coef_im);
+    const double2 nanfill = make_double2(0.0, 0.0);
+    for (int64_t t0 = 0; t0 < nt && e == MGT_OK; t0 += ct) {
+      const int tc = (int)std::min<int64_t>(ct, nt - t0);
+      e = assemble_propagator_into(kind, targets + t0 * dim, tc, sources, ns, k0, mcoef, regularize != 0, radius,
+                                   MGT_NAN_KEEP, nanfill, 0, Gc, (int64_t)d * ns, MGT_CDF, st);
+      if (e != MGT_OK) break;
+      const double2* b = E0 ? (const double2*)E0 + t0 * d * ld_e0 : nullptr;
+      e = residual_rect(Gc, (int64_t)d * ns, Xs, nrhs, b, ld_e0, (double2*)out + t0 * d * ld_out, ld_out, tc * d,
+                        d * ns, (int)nrhs, st, part, (int64_t)prop_part_elems(nt, ns, nrhs, d));
+    }
+    return e;
+  }
   const int nsplit = choose_splits(n_targets, n_sources);
   const int sps = (ns + nsplit - 1) / nsplit;
   const int tiles = (nt + kPT - 1) / kPT;

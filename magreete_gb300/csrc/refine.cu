@@ -23,7 +23,7 @@ template <int RT>
 __global__ void __launch_bounds__(256)
 residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __restrict__ Xs, int64_t ldxs,
                    const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R, int64_t ldr, int n,
-                   int ncols, int col_base) {
+                   int kdim, int ncols, int col_base, int k_per_split, double2* __restrict__ partial) {
   __shared__ float4 Ms[kResRows][kResK + 1];
   __shared__ float4 Xsh[kResK][16 * RT];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -33,19 +33,22 @@ residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __re
   for (int i = 0; i < 2; ++i)
 #pragma unroll
     for (int j = 0; j < RT; ++j) acc[i][j] = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int k0 = 0; k0 < n; k0 += kResK) {
+  // split-K (partial != null): this CTA covers K range [kbeg, kend) and
+  // writes its joined sum to partial[blockIdx.y]
+  const int kbeg = blockIdx.y * k_per_split, kend = min(kdim, kbeg + k_per_split);
+  for (int k0 = kbeg; k0 < kend; k0 += kResK) {
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       int idx = tid + 256 * q;
       int r = idx >> 4, kk = idx & 15;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row0 + r < n && k0 + kk < n) v = M[(int64_t)(row0 + r) * ldm + k0 + kk];
+      if (row0 + r < n && k0 + kk < kend) v = M[(int64_t)(row0 + r) * ldm + k0 + kk];
       Ms[r][kk] = v;
     }
     for (int idx = tid; idx < kResK * 16 * RT; idx += 256) {
       int kk = idx / (16 * RT), c = idx - kk * (16 * RT);
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (k0 + kk < n && c < ncols) v = Xs[(int64_t)(k0 + kk) * ldxs + col_base + c];
+      if (k0 + kk < kend && c < ncols) v = Xs[(int64_t)(k0 + kk) * ldxs + col_base + c];
       Xsh[kk][c] = v;
     }
     __syncthreads();
@@ -69,9 +72,13 @@ residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __re
     for (int j = 0; j < RT; ++j) {
       int c = tx + 16 * j;
       if (c < ncols) {
-        double2 b = B[(int64_t)r * ldb + col_base + c];
         double2 mx = df_join(acc[i][j]);
-        R[(int64_t)r * ldr + col_base + c] = make_double2(b.x - mx.x, b.y - mx.y);
+        if (partial) {
+          partial[((int64_t)blockIdx.y * n + r) * ncols + c] = mx;
+        } else {
+          double2 b = B ? B[(int64_t)r * ldb + col_base + c] : make_double2(0.0, 0.0);
+          R[(int64_t)r * ldr + col_base + c] = make_double2(b.x - mx.x, b.y - mx.y);
+        }
       }
     }
   }
@@ -130,28 +137,97 @@ __global__ void sumsq_kernel(const double2* __restrict__ X, int64_t ldx, int n, 
 
 template <int RT>
 static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B,
-                            int64_t ldb, double2* R, int64_t ldr, int n, int ncols, int col_base, cudaStream_t s) {
+                            int64_t ldb, double2* R, int64_t ldr, int n, int kdim, int ncols, int col_base,
+                            int ksplit, int kps, double2* partial, cudaStream_t s) {
   count_launch();
-  residual_df_kernel<RT><<<(n + kResRows - 1) / kResRows, 256, 0, s>>>(M, ldm, Xs, ldxs, B, ldb, R, ldr, n, ncols,
-                                                                        col_base);
+  dim3 grid((n + kResRows - 1) / kResRows, ksplit);
+  residual_df_kernel<RT><<<grid, 256, 0, s>>>(M, ldm, Xs, ldxs, B, ldb, R, ldr, n, kdim, ncols, col_base, kps,
+                                              partial);
 }
 
-static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb,
-                         double2* R, int64_t ldr, int n, int nrhs, float4* Xs, cudaStream_t s) {
-  int64_t tot = (int64_t)n * nrhs;
-  count_launch();
-  split_df_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ldx, Xs, nrhs, n, nrhs);
+// R = B - sum of the split-K partials (FP64)
+__global__ void residual_reduce_kernel(const double2* __restrict__ partial, int ksplit, int n, int ncols,
+                                       const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R,
+                                       int64_t ldr, int col_base) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * ncols) return;
+  const int r = (int)(idx / ncols), c = (int)(idx - (int64_t)r * ncols);
+  double2 acc = B ? B[(int64_t)r * ldb + col_base + c] : make_double2(0.0, 0.0);
+  for (int q = 0; q < ksplit; ++q) {
+    const double2 v = partial[(int64_t)q * n * ncols + idx];
+    acc.x -= v.x;
+    acc.y -= v.y;
+  }
+  R[(int64_t)r * ldr + col_base + c] = acc;
+}
+
+static int res_num_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  });
+  return sms;
+}
+
+// K splits for a rows x kdim residual: enough CTAs for two waves when the
+// rows alone give fewer, at least 1024 columns of K per split
+int residual_ksplit(int rows, int kdim) {
+  const int rb = (rows + kResRows - 1) / kResRows;
+  const int want = (2 * res_num_sms() + rb - 1) / rb;
+  return std::max(1, std::min({want, kdim / 1024, 32}));
+}
+
+// R (rows x nrhs) = B - M Xs, M (rows x kdim) double-float, Xs (kdim x nrhs,
+// leading dimension ldxs) the double-float copy of X; B may be null (zero).
+// With a partial buffer (partial_elems complex128) the K range is split
+// across CTAs (short, wide M): residual_ksplit(rows, kdim) splits, fewer if
+// the buffer holds fewer than splits x rows x min(nrhs, 128).
+int residual_rect(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B, int64_t ldb,
+                  double2* R, int64_t ldr, int rows, int kdim, int nrhs, cudaStream_t s, double2* partial,
+                  int64_t partial_elems) {
+  int ksplit = partial ? residual_ksplit(rows, kdim) : 1;
+  // never more splits than the partial buffer holds
+  const int64_t per_split = (int64_t)rows * std::min(nrhs, 128);
+  if (per_split > 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(ksplit, partial_elems / per_split));
+  const int kps = ksplit > 1 ? (((kdim + ksplit - 1) / ksplit + kResK - 1) / kResK) * kResK : kdim;
+  double2* part = ksplit > 1 ? partial : nullptr;
   for (int c0 = 0; c0 < nrhs; c0 += 128) {
     int nc = std::min(128, nrhs - c0);
     int rt = (nc + 15) / 16;
     switch (rt) {
-      case 1: launch_residual<1>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
-      case 2: launch_residual<2>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
-      case 3: case 4: launch_residual<4>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
-      default: launch_residual<8>(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, nc, c0, s); break;
+      case 1: launch_residual<1>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
+      case 2: launch_residual<2>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
+      case 3: case 4: launch_residual<4>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
+      default: launch_residual<8>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
+    }
+    if (part) {
+      const int64_t tot = (int64_t)rows * nc;
+      count_launch();
+      residual_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(part, ksplit, rows, nc, B, ldb, R, ldr,
+                                                                           c0);
     }
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+// Xs (n x ncols, leading dimension ldy) = double-float split of X
+int split_df(const double2* X, int64_t ldx, float4* Xs, int64_t ldy, int n, int ncols, cudaStream_t s) {
+  int64_t tot = (int64_t)n * ncols;
+  if (tot <= 0) return MGT_OK;
+  count_launch();
+  split_df_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ldx, Xs, ldy, n, ncols);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+
+static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb,
+                         double2* R, int64_t ldr, int n, int nrhs, float4* Xs, cudaStream_t s) {
+  int e = split_df(X, ldx, Xs, nrhs, n, nrhs, s);
+  if (e != MGT_OK) return e;
+  return residual_rect(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, n, nrhs, s, nullptr, 0);
 }
 
 size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem);

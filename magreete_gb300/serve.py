@@ -76,10 +76,14 @@ def solve_problem(prob, precision="mixed", pts=None, det=None, tol=E.DEFAULT_TOL
 def matrix_bytes(prob, precision="mixed"):
     """Device bytes a request holds at its peak: the matrix copies (24 B / entry
     mixed: complex64 LU + double-float residual copy; 16 B fp64), the
-    tensor-core split buffers (3 KB per row) and the right-hand-side blocks."""
+    tensor-core split buffers (3 KB per row), the right-hand-side blocks and
+    the propagation workspace (double-float propagator rows, at most 1 GiB at
+    a time, and the double-float copy of the fields)."""
     n, R = prob.n, prob.nrhs
     per = 16 if precision == "fp64" else 24
-    return per * n * n + 3072 * n + 8 * 16 * n * R + (64 << 20)
+    T = prob.detectors.shape[0] if prob.detectors is not None else 0
+    prop = min(1 << 30, 16 * prob.d * n * T) + 16 * n * R
+    return per * n * n + 3072 * n + 8 * 16 * n * R + prop + (64 << 20)
 
 
 def serve_sequential(problems, precision="mixed", device_inputs=None, start=None):
