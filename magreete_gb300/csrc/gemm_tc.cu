@@ -53,16 +53,18 @@ namespace tc {
 constexpr int BM = 128;            // tile rows (M)
 constexpr int BN = 128;            // tile real columns (N') = 64 complex columns
 constexpr int KR = 256;            // real K stride of the split buffers (2 * 128 complex)
-constexpr int STAGES = 2;
 constexpr uint32_t A_TILE = BM * 128;      // 16 KB: 128 rows of one 128-byte swizzle row
 constexpr uint32_t B_TILE = BN * 128;      // 16 KB
 constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 64 KB
 constexpr int CHUNKS = BN / 32;            // epilogue chunks per tile (32 fp32 columns each)
-constexpr int CSLOTS = 4;                  // C chunk ring
 constexpr uint32_t CHUNK_BYTES = BM * 128; // 16 KB
 constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int THREADS = 256;
-constexpr size_t SMEM_BYTES = STAGES * STAGE_BYTES + CSLOTS * CHUNK_BYTES + 1024 /* alignment slack */ + 256;
+// pipeline shape: operand stages x C ring slots (2 x 4: 128 + 64 KB)
+template <int STAGES, int CSLOTS>
+constexpr size_t smem_bytes() {
+  return STAGES * STAGE_BYTES + CSLOTS * CHUNK_BYTES + 1024 /* alignment slack */ + 256;
+}
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -173,7 +175,7 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void*
                : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
@@ -190,11 +192,12 @@ __device__ __forceinline__ bool epi_bar_and(bool p) {
 
 // Persistent kernel: each CTA walks tiles blockIdx.x, +gridDim.x, ...; TMEM
 // holds two accumulators so the epilogue of tile t overlaps the MMAs of
-// tile t+1; C moves through a 4-slot ring of 128 x 32 fp32 chunks with TMA
-// loads (prefetched one tile ahead) and TMA stores.
+// tile t+1; C moves through a ring of 128 x 32 fp32 chunks with TMA loads
+// (prefetched CSLOTS - 1 chunks ahead) and TMA stores, a slot being refilled
+// once the store issued before the newest one has read it.
 // invA / invB (F16 mode): inverse row scales of A and inverse complex-column
 // scales of B, relative to the block being updated.
-template <bool F16>
+template <bool F16, int STAGES, int CSLOTS>
 __global__ void __launch_bounds__(THREADS, 1)
 cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                     const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
@@ -341,12 +344,15 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
           tma_store_2d(&mapC, cring + slot * CHUNK_BYTES, x, y);
           bulk_commit();
           processed = g + 1;
-          const int gn = g + CSLOTS;
-          if (gn < ntiles * CHUNKS) {
-            bulk_wait_read0();   // the slot's store has read its data
+          // refill the previous chunk's slot: its store (all but the newest
+          // bulk group) has read its data, while this chunk's store stays in flight
+          const int gn = g - 1 + CSLOTS;
+          if (g >= 1 && gn < ntiles * CHUNKS) {
+            bulk_wait_read1();
             chunk_coords(gn, x, y);
-            mbar_expect_tx(&cfull[slot], CHUNK_BYTES);
-            tma_load_2d(cring + slot * CHUNK_BYTES, &mapC, &cfull[slot], x, y);
+            const int ps = gn % CSLOTS;
+            mbar_expect_tx(&cfull[ps], CHUNK_BYTES);
+            tma_load_2d(cring + ps * CHUNK_BYTES, &mapC, &cfull[ps], x, y);
             issued = gn + 1;
           }
         }
@@ -616,10 +622,10 @@ static int tc_num_sms() {
 static void tc_init_attrs() {
   static std::once_flag once;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::SMEM_BYTES);
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::SMEM_BYTES);
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<2, 4>());
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<2, 4>());
   });
 }
 
@@ -669,14 +675,15 @@ int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, in
   const int total = tiles_n * tiles_m;
   int ctas = std::min(total, max_ctas > 0 ? max_ctas : tc_num_sms());
   count_launch();
+#define MGT_TC_LAUNCH(F16, ST, CS)                                                                              \
+  tc::cgemm_split3_kernel<F16, ST, CS><<<ctas, tc::THREADS, tc::smem_bytes<ST, CS>(), s>>>(                    \
+      plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB, \
+      status)
   if (plan.mode == MGT_TC_F16X2)
-    tc::cgemm_split3_kernel<true><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(
-        plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
-        status);
+    MGT_TC_LAUNCH(true, 2, 4);
   else
-    tc::cgemm_split3_kernel<false><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(
-        plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB,
-        status);
+    MGT_TC_LAUNCH(false, 2, 4);
+#undef MGT_TC_LAUNCH
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 

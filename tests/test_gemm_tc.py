@@ -12,6 +12,7 @@ def rel(a, b):
 
 @pytest.fixture(params=["f16x2", "tf32x3"])
 def tc_mode(request):
+    """split-product scheme of the update kernel"""
     from magreete_gb300 import _lib as L
     lib = L.load()
     old = lib.mgt_get_tuning(L.MGT_TUNE_TC_PRECISION)
