@@ -252,6 +252,11 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        next block's panels on a side stream's spare SMs while
  *                        the rest of the trailing update runs (cooperative
  *                        panels, not under stream capture); 0: strictly in order
+ *   MGT_TUNE_FUSED_RIGHT 1 (default): the complex64 tensor-core LU treats the
+ *                        columns right of each 128-wide block in one pass (both
+ *                        panels' interchanges, solves with the inverted 64 x 64
+ *                        diagonal blocks); 0: two swap passes and a pre-update
+ *                        pass with substitution
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -261,6 +266,7 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_PANEL_REGISTERS 5
 #define MGT_TUNE_TC_PRECISION 6
 #define MGT_TUNE_LOOKAHEAD 7
+#define MGT_TUNE_FUSED_RIGHT 8
 #define MGT_TC_TF32X3 0
 #define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);

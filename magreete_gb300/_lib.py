@@ -29,6 +29,7 @@ MGT_TUNE_PANEL_ROWS, MGT_TUNE_OUTER_BLOCK, MGT_TUNE_PANEL_MAX_CTAS, MGT_TUNE_COO
 MGT_TUNE_PANEL_REGISTERS = 5
 MGT_TUNE_TC_PRECISION = 6
 MGT_TUNE_LOOKAHEAD = 7
+MGT_TUNE_FUSED_RIGHT = 8
 MGT_TC_TF32X3, MGT_TC_F16X2 = 0, 1
 
 _vp = ctypes.c_void_p

@@ -41,10 +41,12 @@ struct LuWsLayout {
   size_t epoch = 40;      // u64: factorisation counter (bumped on the device, never cleared)
   size_t slots = 64;      // 2 sets x 2*NBmax x int2 (pos, src)
   size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
+  size_t inv;             // 2 x NBmax x NBmax complex: inverses of a 128-wide block's diagonal blocks
   size_t total;
   LuWsLayout() {
     records = (slots + 2 * 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
-    total = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
+    inv = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
+    total = inv + 2 * (size_t)kNBmax * kNBmax * sizeof(double2);
   }
 };
 
@@ -640,6 +642,7 @@ static std::atomic<int> g_panel_max_ctas{0};     // 0: one per SM
 static std::atomic<int> g_cooperative{1};        // panel launched with the cooperative attribute
 static std::atomic<int> g_panel_reg{1};          // register-resident panel: 0 never, 1 complex64, 2 both
 static std::atomic<int> g_lookahead{1};          // tensor-core LU: next block's panels beside the update
+static std::atomic<int> g_fused_right{1};        // tensor-core LU: one fused pass for a block's right columns
 
 // Row interchanges for the columns outside the panel, then (right of the
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
@@ -757,6 +760,158 @@ lu_preupdate_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, in
   for (int idx = tid; idx < wb * kSwapCols; idx += 256) {
     int r = idx / kSwapCols, cc = idx - r * kSwapCols;
     if (cc < ncols) A[(int64_t)(j1 + r) * lda + col0 + cc] = buf[r * kSwapCols + cc];
+  }
+}
+
+template <typename T>
+int lower_block_inverses(const cplx<T>* F, int64_t ldf, int n, cplx<T>* Inv, cudaStream_t s);
+
+// dynamic shared memory of lu_block_right_kernel: block rows, moved rows, one operator
+template <int NB>
+constexpr size_t block_right_smem(size_t elem) {
+  return ((size_t)2 * NB * kSwapCols + (size_t)4 * NB * kSwapCols + (size_t)NB * (NB + 1)) * elem;
+}
+
+// Columns right of a 128-wide block whose inner panels sit at J0 (width wa)
+// and j1 = J0 + wa (width wb), in one pass per 32 columns: both panels' row
+// interchanges (slot sets A and B, composed), then U_A = L_AA^-1 X_A,
+// X_B -= L_BA U_A and U_B = L_BB^-1 X_B with the diagonal blocks' inverses
+// precomputed (Inv[0] = L_AA^-1, Inv[1] = L_BB^-1).  The same arithmetic as
+// the two swap passes and the pre-update pass it replaces, with the
+// triangular solves as products with the inverses.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256)
+lu_block_right_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, int wa, int wb, int col_begin,
+                      PanelWs wsA, PanelWs wsB, const cplx<T>* __restrict__ Inv) {
+  using V = cplx<T>;
+  constexpr int CW = kSwapCols;
+  constexpr int MAXF = 4 * NB;                 // moved rows below the block (both slot sets)
+  static_assert(NB == 64 && CW == 32 && 256 == 4 * NB, "thread tiling: 32 x 2 rows, 8 x 4 columns");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* Tb = reinterpret_cast<V*>(smem_raw);      // [2 NB][CW] the block's rows
+  V* Fr = Tb + 2 * NB * CW;                    // [MAXF][CW] moved rows below the block
+  V* Lb = Fr + MAXF * CW;                      // [NB][NB + 1] operator of the current step
+  __shared__ int tsrc[2 * NB];                 // source (rel J0) of each block row
+  __shared__ int fpos[MAXF], fsrc[MAXF];       // moved rows below the block: position, source (rel J0)
+  __shared__ int s_nf;
+  const int tid = threadIdx.x;
+  const int W = wa + wb;
+  const int col0 = col_begin + blockIdx.x * CW;
+  const int ncols = min(CW, n - col0);
+  const int m = n - J0;
+  const int nsA = min(*wsA.nslot, 2 * NB);
+  const int nsB = wb > 0 ? min(*wsB.nslot, 2 * NB) : 0;
+  // source (rel J0) of position x (rel J0) after panel A's interchanges
+  auto srcA = [&](int x) -> int {
+    if (x < NB) return x < nsA ? wsA.slots[x].y : x;
+    for (int q = NB; q < nsA; ++q)
+      if (wsA.slots[q].x == x) return wsA.slots[q].y;
+    return x;
+  };
+  // source (rel J0) of position p (rel J0) after both panels' interchanges
+  auto src_both = [&](int p) -> int {
+    int mid = p;
+    if (wb > 0 && p >= wa) {
+      const int y = p - wa;
+      if (y < NB) {
+        if (y < nsB) mid = wsB.slots[y].y + wa;
+      } else {
+        for (int q = NB; q < nsB; ++q)
+          if (wsB.slots[q].x == y) { mid = wsB.slots[q].y + wa; break; }
+      }
+    }
+    return srcA(mid);
+  };
+  if (tid == 0) s_nf = 0;
+  __syncthreads();
+  // positions below the block that either panel touches: A's (rel J0) and B's (rel j1)
+  for (int q = tid; q < nsA + nsB; q += blockDim.x) {
+    const bool isA = q < nsA;
+    const int2 sl = isA ? wsA.slots[q] : wsB.slots[q - nsA];
+    const int p = isA ? sl.x : sl.x + wa;
+    if (p < W || p >= m) continue;
+    bool dup = false;
+    if (!isA)   // a position in both lists is taken from A's
+      for (int r = 0; r < nsA && !dup; ++r) dup = wsA.slots[r].x == p;
+    if (!dup) {
+      const int k = atomicAdd(&s_nf, 1);
+      if (k < MAXF) fpos[k] = p;
+    }
+  }
+  for (int r = tid; r < W; r += blockDim.x) tsrc[r] = src_both(r);
+  __syncthreads();
+  const int nf = min(s_nf, MAXF);
+  for (int f = tid; f < nf; f += blockDim.x) fsrc[f] = src_both(fpos[f]);
+  __syncthreads();
+  // gather every source before anything is written
+  for (int idx = tid; idx < 2 * NB * CW; idx += blockDim.x) {
+    const int r = idx / CW, c = idx - r * CW;
+    Tb[idx] = (r < W && c < ncols) ? A[(int64_t)(J0 + tsrc[r]) * lda + col0 + c] : czero<V>();
+  }
+  for (int idx = tid; idx < nf * CW; idx += blockDim.x) {
+    const int f = idx / CW, c = idx - f * CW;
+    if (c < ncols) Fr[idx] = A[(int64_t)(J0 + fsrc[f]) * lda + col0 + c];
+  }
+  for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+    const int r = idx / NB, k = idx - r * NB;
+    Lb[r * (NB + 1) + k] = Inv[idx];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nf * CW; idx += blockDim.x) {
+    const int f = idx / CW, c = idx - f * CW;
+    if (c < ncols) A[(int64_t)(J0 + fpos[f]) * lda + col0 + c] = Fr[idx];
+  }
+  // Y (NB rows of Tb from row0) = Lb * Y, or Y -= Lb * X (X = the first NB
+  // rows); each thread a 2 x 4 tile: rows 2 tr, 2 tr + 1, columns tc + 8 j
+  auto apply = [&](int row0, bool sub) {
+    const int tr = tid >> 3, tc = tid & 7;
+    const V* X = sub ? Tb : Tb + row0 * CW;
+    V acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = sub ? Tb[(row0 + 2 * tr + i) * CW + tc + 8 * j] : czero<V>();
+#pragma unroll 4
+    for (int k = 0; k < NB; ++k) {
+      const V l0 = Lb[(2 * tr) * (NB + 1) + k], l1 = Lb[(2 * tr + 1) * (NB + 1) + k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const V x = X[k * CW + tc + 8 * j];
+        if (sub) {
+          cfms(acc[0][j], l0, x);
+          cfms(acc[1][j], l1, x);
+        } else {
+          cfma(acc[0][j], l0, x);
+          cfma(acc[1][j], l1, x);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Tb[(row0 + 2 * tr + i) * CW + tc + 8 * j] = acc[i][j];
+    __syncthreads();
+  };
+  apply(0, false);                                   // U_A = L_AA^-1 X_A
+  if (wb > 0) {
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+      const int r = idx / NB, k = idx - r * NB;
+      Lb[r * (NB + 1) + k] = (r < wb && k < wa) ? A[(int64_t)(J0 + wa + r) * lda + J0 + k] : czero<V>();
+    }
+    __syncthreads();
+    apply(NB, true);                                 // X_B -= L_BA U_A
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+      const int r = idx / NB, k = idx - r * NB;
+      Lb[r * (NB + 1) + k] = Inv[NB * NB + idx];
+    }
+    __syncthreads();
+    apply(NB, false);                                // U_B = L_BB^-1 X_B
+  }
+  for (int idx = tid; idx < W * CW; idx += blockDim.x) {
+    const int r = idx / CW, c = idx - r * CW;
+    const int rr = r < wa ? r : NB + (r - wa);
+    if (c < ncols) A[(int64_t)(J0 + r) * lda + col0 + c] = Tb[rr * CW + c];
   }
 }
 
@@ -934,6 +1089,9 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   const size_t sm3 = (NB * kSwapCols + NB * (NB + 1) + NB * kSwapCols) * sizeof(V);
   std::call_once(once2, [sm3] {
     cudaFuncSetAttribute(lu_preupdate_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    if constexpr (sizeof(T) == 4)
+      cudaFuncSetAttribute(lu_block_right_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)block_right_smem<NB>(sizeof(V)));
   });
   // Lookahead (cooperative panels, not under stream capture): the trailing
   // update of block J0 first brings the next block's columns up to date, then
@@ -970,6 +1128,16 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int W = std::min(2 * NB, n - J0), wa = std::min(NB, W), wb = W - wa, j1 = J0 + wa;
     const int right = n - J0 - W;
     if (right <= 0) return;
+    if constexpr (sizeof(T) == 4) {
+      if (wb > 0 && g_fused_right.load(std::memory_order_relaxed)) {
+        V* Inv = reinterpret_cast<V*>((char*)work + LuWsLayout().inv);
+        lower_block_inverses<T>(A + (int64_t)J0 * lda + J0, lda, W, Inv, s);
+        lu_block_right_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, block_right_smem<NB>(sizeof(V)), s>>>(
+            A, lda, n, J0, wa, wb, J0 + W, panel_ws(work, 0), panel_ws(work, 1), Inv);
+        count_launch();
+        return;
+      }
+    }
     swap(s, J0, wa, 0, 0, J0 + W, n, 1);
     if (wb > 0) {
       swap(s, j1, wb, 1, 0, J0 + W, n, 0);
@@ -1328,6 +1496,10 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_lookahead.store(value ? 1 : 0);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_FUSED_RIGHT) {
+    g_fused_right.store(value ? 1 : 0);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
@@ -1339,5 +1511,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_PANEL_REGISTERS) return g_panel_reg.load();
   if (key == MGT_TUNE_TC_PRECISION) return tc_get_mode();
   if (key == MGT_TUNE_LOOKAHEAD) return g_lookahead.load();
+  if (key == MGT_TUNE_FUSED_RIGHT) return g_fused_right.load();
   return MGT_ERR_ARG;
 }

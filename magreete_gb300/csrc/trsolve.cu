@@ -177,10 +177,17 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
   }
 }
 
-// counter = 0 for the work-item claims; epoch += 1
-__global__ void tri_start_kernel(unsigned* counter, unsigned* epoch) {
-  *counter = 0;
-  *epoch += 1;
+// counter = 0 for the work-item claims; every completion flag of this solve
+// cleared and the completion mark set to 1.  The workspace is allocated by the
+// caller and may hold anything (a freed permutation holds every small
+// integer), so nothing of the protocol may depend on its previous contents.
+__global__ void tri_start_kernel(unsigned* counter, unsigned* mark, unsigned* flags, int nflags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *counter = 0;
+    *mark = 1;
+  }
+  for (int f = i; f < nflags; f += gridDim.x * blockDim.x) flags[f] = 0;
 }
 
 // counter + status (256 B), flags (groups x blocks), inverted diagonal blocks (L and U)
@@ -219,14 +226,31 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   V* inv = (V*)((char*)work + 256 + flag_bytes) + (UPPER ? (size_t)nb * kTB * kTB : 0);
   count_launch();
   diag_inverse_kernel<T, UPPER><<<nb, 256, smem_inv, s>>>(F, ldf, n, inv);
-  unsigned* epoch = counter + 1;   // never cleared: it only has to change between solves
+  unsigned* epoch = counter + 1;   // completion mark, set by tri_start_kernel
   count_launch();
-  tri_start_kernel<<<1, 1, 0, s>>>(counter, epoch);
+  tri_start_kernel<<<std::max(1, std::min(nb * ng, 1 << 16) / 256 + 1), 256, 0, s>>>(counter, epoch, flags, nb * ng);
   count_launch();
   const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
   tri_solve_kernel<T, UPPER><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch, status);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
+
+// Inverses of the 64 x 64 diagonal blocks of a unit lower factor of order n
+// (rows / columns at F), written to Inv[block][64][64]; the LU uses it for the
+// two inner panels of a 128-wide block.
+template <typename T>
+int lower_block_inverses(const cplx<T>* F, int64_t ldf, int n, cplx<T>* Inv, cudaStream_t s) {
+  using V = cplx<T>;
+  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
+  static std::once_flag once;
+  std::call_once(once, [smem_inv] {
+    cudaFuncSetAttribute(diag_inverse_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
+  });
+  count_launch();
+  diag_inverse_kernel<T, false><<<(n + kTB - 1) / kTB, 256, smem_inv, s>>>(F, ldf, n, Inv);
+  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+}
+template int lower_block_inverses<float>(const float2*, int64_t, int, float2*, cudaStream_t);
 
 template int tri_solve<double, false>(const double2*, int64_t, double2*, int64_t, int, int, void*, int*, cudaStream_t);
 template int tri_solve<double, true>(const double2*, int64_t, double2*, int64_t, int, int, void*, int*, cudaStream_t);

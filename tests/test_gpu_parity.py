@@ -227,6 +227,72 @@ def test_lookahead_matches_in_order(n):
     assert torch.equal(outs[0][0], outs[1][0])
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1000, 4000])
+def test_fused_block_right_matches_passes(n):
+    """The fused pass over a 128-wide block's right columns (composed
+    interchanges, solves with inverted diagonal blocks) is a valid factorisation
+    (P A = L U to FP32 rounding) and picks the same pivots as the three-pass
+    version while the two have not drifted apart: the same arithmetic in
+    another order differs by FP32 rounding, which can flip a near-tie among the
+    last columns' few candidates, so exact agreement is required for the first
+    four blocks only."""
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    lib = L.load()
+    gen = torch.Generator().manual_seed(n + 29)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen).to(torch.complex64)
+    outs = []
+    try:
+        for mode in (0, 1):
+            lib.mgt_set_tuning(L.MGT_TUNE_FUSED_RIGHT, mode)
+            f = E.lu_factor(A.cuda().clone(), check_singular=False)
+            torch.cuda.synchronize()
+            outs.append((f.lu.cpu().to(torch.complex128), f.perm.cpu()))
+    finally:
+        lib.mgt_set_tuning(L.MGT_TUNE_FUSED_RIGHT, 1)
+    assert torch.equal(outs[0][1][:512], outs[1][1][:512])
+    LU = outs[1][0]
+    Lm = torch.tril(LU, -1) + torch.eye(n, dtype=torch.complex128)
+    PA = A.to(torch.complex128)[outs[1][1].long()]
+    assert rel(Lm @ torch.triu(LU), PA) < 5e-8 * n
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
+@pytest.mark.parametrize("fill", ["iota", "small_ints", "ones"])
+def test_lu_solve_any_workspace_contents(dtype, fill):
+    """The triangular solves' completion flags live in the caller's workspace:
+    whatever it held before (a freed permutation holds every small integer)
+    must not mark a block as solved."""
+    import ctypes
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    lib = L.load()
+    n, R = 1500, 40
+    gen = torch.Generator().manual_seed(3)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen) + 40 * torch.eye(n)
+    B = torch.randn(n, R, dtype=torch.complex128, generator=gen)
+    f = E.lu_factor(A.to(dtype).cuda())
+    nb = ctypes.c_size_t()
+    L.check(lib.mgt_lu_solve_workspace_bytes(f.dtype_code, n, R, ctypes.byref(nb)))
+    words = (nb.value + 3) // 4
+    if fill == "iota":
+        work = torch.arange(words, dtype=torch.int32, device="cuda")
+    elif fill == "small_ints":
+        work = torch.arange(words, dtype=torch.int32, device="cuda") % 7
+    else:
+        work = torch.ones(words, dtype=torch.int32, device="cuda")
+    Bd = B.to(dtype).cuda().contiguous()
+    X = torch.empty_like(Bd)
+    L.check(lib.mgt_lu_solve(f.dtype_code, ctypes.c_void_p(f.lu.data_ptr()), n, f.lu.stride(0),
+                             ctypes.c_void_p(f.perm.data_ptr()), ctypes.c_void_p(Bd.data_ptr()), R,
+                             ctypes.c_void_p(X.data_ptr()), R, R, ctypes.c_void_p(work.data_ptr()), work.numel() * 4,
+                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    ref = torch.linalg.solve(A.to(dtype).to(torch.complex128), B.to(dtype).to(torch.complex128))
+    assert rel(X.cpu().to(torch.complex128), ref) < (1e-12 if dtype == torch.complex128 else 1e-4)
+
+
 def test_singular_matrix_raises():
     from magreete_gb300 import engine as E
     A = torch.randn(80, 80, dtype=torch.complex128)
