@@ -39,9 +39,10 @@ WORKLOAD = ("serving stream (continuous batching, 4 requests in flight): Poisson
             "k0L U[2pi*5, 2pi*25], 1-64 RHS, 20% geometry re-queries at a new k0; mixed method refined to 1e-10; "
             "detectors 360 ring (2D) / 1024 Fibonacci sphere (3D)")
 METRIC = "solves/s (mixed-N 2D/3D request stream, refined to 1e-10 relative residual)"
-# DRAM bytes / algorithmic bytes of the trailing update, from an ncu capture of one launch
-# (3D N=4000, M = N = 11680, K = 64: 2.287 GB of DRAM traffic vs 2.25 GB algorithmic)
-TRAFFIC_RATIO = 1.02
+# DRAM bytes / algorithmic bytes of the trailing update, from an ncu capture of one
+# full-size launch (3D N=4000, M = 11264, N = 11136 complex, K = 128: 2.009 GB of DRAM
+# traffic vs 2.03 GB algorithmic)
+TRAFFIC_RATIO = 0.99
 
 
 def parse():
