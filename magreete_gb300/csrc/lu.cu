@@ -455,11 +455,9 @@ lu_panel_reg_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, 
       const bool wc = tc >= 0 && (tc >> 5) == warp;
       if (wb || wc) {
         if (tid == tb || tid == tc) {
+          // branch-free: columns past the panel go to the row's pad column (index NB)
 #pragma unroll
-          for (int k = 0; k < NB; ++k) {
-            if (c + k >= w) break;
-            sL[tid * LD + c + k] = a[k];
-          }
+          for (int k = 0; k < NB; ++k) sL[tid * LD + min(c + k, NB)] = a[k];
         }
         __syncwarp();
         V* rec = reinterpret_cast<V*>(my + kRecHeader);
@@ -471,8 +469,10 @@ lu_panel_reg_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, 
     }
     __syncthreads();
     const unsigned tag = (unsigned)((j0 + c) & 127) + 1u;
+    // the release store orders every row write of the CTA before it: the
+    // writes precede the barrier above, which thread 0 has passed (PTX
+    // release patterns are cumulative over causality order)
     if (tid == 0) {
-      __threadfence();
       if (PK::kPacked)
         st_release_u64(reinterpret_cast<unsigned long long*>(my), pack_flag(tag, s_best, (unsigned)s_bkey));
       else
