@@ -257,6 +257,10 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        panels' interchanges, solves with the inverted 64 x 64
  *                        diagonal blocks); 0: two swap passes and a pre-update
  *                        pass with substitution
+ *   MGT_TUNE_PANEL_CLUSTER 1 (default): complex64 register panels of at most 16
+ *                        CTAs (8 where the device schedules no larger cluster)
+ *                        run as one thread-block cluster and exchange pivots
+ *                        through distributed shared memory; 0: through L2
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -267,6 +271,7 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_TC_PRECISION 6
 #define MGT_TUNE_LOOKAHEAD 7
 #define MGT_TUNE_FUSED_RIGHT 8
+#define MGT_TUNE_PANEL_CLUSTER 9
 #define MGT_TC_TF32X3 0
 #define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);

@@ -633,6 +633,261 @@ lu_panel_reg_kernel(cplx<T>* __restrict__ A, int64_t lda, int m, int w, int j0, 
 
 constexpr size_t reg_panel_smem(int nb, size_t elem) { return (size_t)kPanelThreads * (nb + 1) * elem; }
 
+// Cluster variant of the register-resident panel, for panels whose CTAs fit
+// in one thread-block cluster (at most 16): the exchange goes through
+// distributed shared memory instead of L2.  Per column each CTA stores its
+// candidate (key, row) into every CTA's table (st.shared::cluster), one
+// hardware cluster barrier makes all tables complete, every CTA picks the
+// same pivot, and the pivot row and row c are read straight from the owning
+// CTAs' shared memory.  Candidate rows and tables alternate between two
+// buffers by column parity, so one barrier per column suffices: a CTA writes
+// buffer b again only after the next column's barrier, which every CTA
+// reaches after its reads of buffer b.  All CTAs run the same barrier
+// sequence (no early exit), and a final barrier keeps every CTA's shared
+// memory alive until the others have read it.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t cluster_map(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cluster_st_u32(uint32_t a, uint32_t v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void cluster_st_u64(uint32_t a, unsigned long long v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long cluster_ld_u64(uint32_t a) {
+  unsigned long long v;
+  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+constexpr int kMaxClusterCtas = 16;
+
+template <int NB>
+__global__ void __launch_bounds__(kPanelThreads, 1)
+lu_panel_cluster_kernel(float2* __restrict__ A, int64_t lda, int m, int w, int j0, int rows_per_cta,
+                        int32_t* __restrict__ perm, PanelWs ws) {
+  using T = float;
+  using V = float2;
+  using PK = PanelKey<T>;
+  using K = typename PK::K;
+  constexpr int LD = NB + 1;
+  constexpr int kNone = 0x7fffffff;
+  constexpr int kChunk = NB < 16 ? NB : 16;
+  extern __shared__ __align__(16) unsigned char panel_smem[];
+  V* sL = reinterpret_cast<V*>(panel_smem);
+  __shared__ V U[2 * NB];
+  __shared__ V RC[2 * NB];
+  __shared__ __align__(16) V rowbuf[2][NB];        // this CTA's candidate row, per column parity
+  __shared__ __align__(16) V rcbuf[2][NB];         // row c (owner CTA), per column parity
+  __shared__ unsigned long long ctab[2][kMaxClusterCtas];   // every CTA's candidate: key << 32 | row + 1
+  __shared__ K red_key[kPanelThreads / 32];
+  __shared__ int red_idx[kPanelThreads / 32];
+  __shared__ K s_bkey;
+  __shared__ int s_best, s_p;
+  __shared__ int s_piv[NB];
+  __shared__ int slot_pos[2 * NB], slot_src[2 * NB];
+  __shared__ int s_nslot;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nwarps = kPanelThreads / 32;
+  const int G = gridDim.x;
+  const int bid = (int)cluster_rank();             // one cluster spans the grid
+  const int r0 = bid * rows_per_cta;
+  const int nr = max(0, min(m, r0 + rows_per_cta) - r0);
+  const int row = r0 + tid;
+  const bool have = tid < nr;
+
+  for (int i = tid; i < 2 * NB; i += kPanelThreads) {
+    U[i] = czero<V>();
+    RC[i] = czero<V>();
+  }
+  for (int i = tid; i < nr * NB; i += kPanelThreads) {
+    const int r = i / NB, k = i % NB;
+    sL[r * LD + k] = k < w ? A[(int64_t)(r0 + r) * lda + k] : czero<V>();
+  }
+  __syncthreads();
+  V a[NB];
+#pragma unroll
+  for (int k = 0; k < NB; ++k) a[k] = have ? sL[tid * LD + k] : czero<V>();
+
+  for (int c = 0; c < w; ++c) {
+    const int buf = c & 1;
+    // ---- 1. this CTA's candidate
+    K key = (have && row >= c) ? PK::key(cabs1(a[0])) : K(0);
+    int bidx = key ? row : kNone;
+    warp_argmax(key, bidx);
+    if (lane == 0) { red_key[warp] = key; red_idx[warp] = bidx; }
+    __syncthreads();
+    if (warp == 0) {
+      key = lane < nwarps ? red_key[lane] : K(0);
+      bidx = lane < nwarps ? red_idx[lane] : kNone;
+      warp_argmax(key, bidx);
+      if (lane == 0) {
+        s_best = key ? bidx : -1;
+        s_bkey = key;
+      }
+    }
+    __syncthreads();
+    // ---- 2. candidate row and (owner) row c into this CTA's buffers; the
+    // candidate into every CTA's table
+    const int tb = s_best >= 0 ? s_best - r0 : -1;
+    const int tc = (c >= r0 && c < r0 + nr) ? c - r0 : -1;
+    {
+      const bool wb = tb >= 0 && (tb >> 5) == warp;
+      const bool wc = tc >= 0 && (tc >> 5) == warp;
+      if (wb || wc) {
+        if (tid == tb || tid == tc) {
+#pragma unroll
+          for (int k = 0; k < NB; ++k) sL[tid * LD + min(c + k, NB)] = a[k];
+        }
+        __syncwarp();
+        if (wb)
+          for (int k = lane; k < NB; k += 32) rowbuf[buf][k] = k < w ? sL[tb * LD + k] : czero<V>();
+        if (wc)
+          for (int k = lane; k < NB; k += 32) rcbuf[buf][k] = k < w ? sL[tc * LD + k] : czero<V>();
+      }
+    }
+    if (warp == 1 && lane < G) {
+      const unsigned long long ent = ((unsigned long long)(unsigned)s_bkey << 32) | (unsigned)(s_best + 1);
+      cluster_st_u64(cluster_map(smem_addr(&ctab[buf][bid]), (uint32_t)lane), ent);
+    }
+    cluster_barrier();
+    // ---- 3. the global pivot, the same in every CTA
+    if (warp == 0) {
+      K bk = 0;
+      int bi = kNone;
+      if (lane < G) {
+        const unsigned long long ent = ctab[buf][lane];
+        bk = (K)(ent >> 32);
+        bi = bk ? (int)(unsigned)(ent & 0xffffffffu) - 1 : kNone;
+      }
+      warp_argmax(bk, bi);
+      if (lane == 0) s_p = bk ? bi : -1;
+    }
+    __syncthreads();
+    const int p = s_p >= 0 ? s_p : c;
+    const int wbk = s_p >= 0 ? s_p / rows_per_cta : -1;
+    const int owner = c / rows_per_cta;
+    // ---- 4. pivot row and row c from the owning CTAs' shared memory
+    for (int i = tid; i < 2 * NB; i += kPanelThreads) {
+      V rc = czero<V>(), u = czero<V>();
+      if (i < w) {
+        const unsigned long long vr = cluster_ld_u64(cluster_map(smem_addr(&rcbuf[buf][i]), (uint32_t)owner));
+        rc = make_float2(__uint_as_float((unsigned)vr), __uint_as_float((unsigned)(vr >> 32)));
+        if (wbk >= 0) {
+          const unsigned long long vu = cluster_ld_u64(cluster_map(smem_addr(&rowbuf[buf][i]), (uint32_t)wbk));
+          u = make_float2(__uint_as_float((unsigned)vu), __uint_as_float((unsigned)(vu >> 32)));
+        } else {
+          u = rc;
+        }
+      }
+      RC[i] = rc;
+      U[i] = u;
+    }
+    __syncthreads();
+    const V piv = U[c];
+    const bool nz = (piv.x != 0 || piv.y != 0);
+    // ---- 5. interchange rows c and p
+    if (nz && p != c) {
+      const int tp = (p >= r0 && p < r0 + nr) ? p - r0 : -1;
+      if (tid < c) {
+        if (tp >= 0) sL[tp * LD + tid] = RC[tid];
+        if (tc >= 0) sL[tc * LD + tid] = U[tid];
+      }
+      if (tid == tp || tid == tc) {
+        const V* src = tid == tp ? RC : U;
+#pragma unroll
+        for (int kc = 0; kc < NB; kc += kChunk) {
+          if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+          for (int k = kc; k < kc + kChunk; ++k) a[k] = src[c + k];
+        }
+      }
+    }
+    if (bid == 0 && tid == 0) {
+      s_piv[c] = nz ? p : c;
+      if (!nz && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
+    }
+    // ---- 6. scale and rank-1 update in registers, retire column c, shift
+    if (have && row > c && nz) {
+      const V l = cmul(a[0], crecip(piv));
+      a[0] = l;
+#pragma unroll
+      for (int kc = 0; kc < NB; kc += kChunk) {
+        if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+        for (int k = (kc ? kc : 1); k < kc + kChunk; ++k) cfms(a[k], l, U[c + k]);
+      }
+    }
+    if (have) sL[tid * LD + c] = a[0];
+#pragma unroll
+    for (int kc = 0; kc < NB; kc += kChunk) {
+      if (kc > 0 && c + kc >= w) break;
+#pragma unroll
+      for (int k = kc; k < kc + kChunk && k + 1 < NB; ++k) a[k] = a[k + 1];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < nr * NB; i += kPanelThreads) {
+    const int r = i / NB, k = i % NB;
+    if (k < w) A[(int64_t)(r0 + r) * lda + k] = sL[r * LD + k];
+  }
+  if (bid == 0 && warp == 0) {
+    for (int s2 = lane; s2 < NB; s2 += 32) { slot_pos[s2] = s2; slot_src[s2] = s2; }
+    if (lane == 0) s_nslot = NB;
+    __syncwarp();
+    for (int s2 = 0; s2 < w; ++s2) {
+      const int pv = s_piv[s2];
+      if (pv == s2) continue;
+      int slot = -1;
+      if (pv < NB) {
+        slot = pv;
+      } else {
+        const int ns = s_nslot;
+        for (int base = NB; base < ns && slot < 0; base += 32) {
+          int q = base + lane;
+          unsigned hit = __ballot_sync(0xffffffffu, q < ns && slot_pos[q] == pv);
+          if (hit) slot = base + __ffs(hit) - 1;
+        }
+        if (slot < 0) {
+          slot = ns;
+          if (lane == 0) { slot_pos[ns] = pv; slot_src[ns] = pv; s_nslot = ns + 1; }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) { int t2 = slot_src[s2]; slot_src[s2] = slot_src[slot]; slot_src[slot] = t2; }
+      __syncwarp();
+    }
+    const int ns = s_nslot;
+    for (int q = lane; q < ns; q += 32) ws.slots[q] = make_int2(slot_pos[q], slot_src[q]);
+    if (lane == 0) *ws.nslot = ns;
+    int32_t pv[2 * NB / 32];
+#pragma unroll
+    for (int j = 0; j < 2 * NB / 32; ++j) {
+      const int q = lane + 32 * j;
+      if (q < ns) pv[j] = perm[j0 + slot_src[q]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 2 * NB / 32; ++j) {
+      const int q = lane + 32 * j;
+      if (q < ns) perm[j0 + slot_pos[q]] = pv[j];
+    }
+  }
+  cluster_barrier();   // no CTA leaves while another may still read its shared memory
+}
+
 constexpr int kSwapCols = 32;
 
 // run-time tuning knobs (set by the autotuner; see mgt_set_tuning)
@@ -954,6 +1209,42 @@ static int trailing_update(const TcLU* tc, int M, int N, int K, const float2* A,
   return gemm_sub<float>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
 
+static std::atomic<int> g_panel_cluster{1};     // complex64 panels of <= 16 CTAs as one cluster
+
+// Largest cluster of register panel CTAs the device schedules (16, 8 or 0).
+static int cluster_panel_max() {
+  static int cmax = -1;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const size_t smem = reg_panel_smem(64, sizeof(float2));
+    cmax = 0;
+    if (cudaFuncSetAttribute(lu_panel_cluster_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return;
+    cudaFuncSetAttribute(lu_panel_cluster_kernel<64>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int size : {kMaxClusterCtas, 8}) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(size);
+      cfg.blockDim = dim3(kPanelThreads);
+      cfg.dynamicSmemBytes = smem;
+      cudaLaunchAttribute a[1];
+      a[0].id = cudaLaunchAttributeClusterDimension;
+      a[0].val.clusterDim.x = size;
+      a[0].val.clusterDim.y = 1;
+      a[0].val.clusterDim.z = 1;
+      cfg.attrs = a;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&clusters, lu_panel_cluster_kernel<64>, &cfg) == cudaSuccess && clusters > 0) {
+        cmax = size;
+        break;
+      }
+    }
+    cudaGetLastError();
+  });
+  return cmax;
+}
+
 // Per-thread side stream and fork / join events for the lookahead update.
 struct SideStream {
   cudaStream_t s = nullptr;
@@ -1021,10 +1312,29 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     // Without the attribute (CUDA-graph capture of concurrent branches) the
     // caller keeps the panels' total CTA count within the SM count instead.
     cfg.numAttrs = g_cooperative.load(std::memory_order_relaxed) ? 1 : 0;
-    // up to one row per thread: the register-resident kernel
+    // up to one row per thread: the register-resident kernel, as one thread-
+    // block cluster (exchange in distributed shared memory) when it fits
     cudaError_t le;
     const int reg_mode = g_panel_reg.load(std::memory_order_relaxed);
-    if (rpc <= kPanelThreads && (reg_mode == 2 || (reg_mode == 1 && sizeof(T) == 4))) {
+    bool launched = false;
+    if constexpr (sizeof(T) == 4) {
+      const int cmax = cluster_panel_max();
+      if (rpc <= kPanelThreads && reg_mode != 0 && G <= cmax && g_panel_cluster.load(std::memory_order_relaxed)) {
+        cudaLaunchConfig_t cc = cfg;
+        cudaLaunchAttribute ca[1];
+        ca[0].id = cudaLaunchAttributeClusterDimension;
+        ca[0].val.clusterDim.x = G;
+        ca[0].val.clusterDim.y = 1;
+        ca[0].val.clusterDim.z = 1;
+        cc.attrs = ca;
+        cc.numAttrs = 1;
+        cc.dynamicSmemBytes = reg_panel_smem(NB, sizeof(V));
+        le = cudaLaunchKernelEx(&cc, lu_panel_cluster_kernel<NB>, P, lda, m, w, j0, rpc, perm, pw);
+        launched = true;
+      }
+    }
+    if (launched) {
+    } else if (rpc <= kPanelThreads && (reg_mode == 2 || (reg_mode == 1 && sizeof(T) == 4))) {
       cfg.dynamicSmemBytes = reg_panel_smem(NB, sizeof(V));
       le = cudaLaunchKernelEx(&cfg, lu_panel_reg_kernel<T, NB>, P, lda, m, w, j0, rpc, perm, pw);
     } else {
@@ -1500,6 +1810,10 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_fused_right.store(value ? 1 : 0);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_PANEL_CLUSTER) {
+    g_panel_cluster.store(value ? 1 : 0);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
@@ -1512,5 +1826,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_TC_PRECISION) return tc_get_mode();
   if (key == MGT_TUNE_LOOKAHEAD) return g_lookahead.load();
   if (key == MGT_TUNE_FUSED_RIGHT) return g_fused_right.load();
+  if (key == MGT_TUNE_PANEL_CLUSTER) return g_panel_cluster.load();
   return MGT_ERR_ARG;
 }

@@ -169,11 +169,13 @@ def test_lu_random(n, dtype):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("dtype", [torch.complex64, torch.complex128])
-@pytest.mark.parametrize("n,rows", [(700, 256), (3000, 64), (5000, 128)])
+@pytest.mark.parametrize("n,rows", [(700, 256), (3000, 64), (5000, 128), (3000, 256), (4000, 256)])
 def test_panel_kernels_agree(n, rows, dtype):
-    """The register-resident panel (one row per thread, integer pivot keys,
-    packed flags for complex64) and the shared-memory panel pick the same
-    pivots and produce bit-identical factors; many CTAs per panel at rows=64."""
+    """The shared-memory panel, the register-resident panel exchanging through
+    L2 (integer pivot keys, packed flags for complex64) and, for complex64
+    panels of at most 16 CTAs, the register panel as one thread-block cluster
+    (exchange in distributed shared memory) pick the same pivots and produce
+    bit-identical factors; many CTAs per panel at rows=64."""
     from magreete_gb300 import _lib as L
     from magreete_gb300 import engine as E
     lib = L.load()
@@ -185,15 +187,18 @@ def test_panel_kernels_agree(n, rows, dtype):
     old_rows = lib.mgt_get_tuning(L.MGT_TUNE_PANEL_ROWS)
     try:
         lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, rows)
-        for mode in (0, 2):
+        for mode, cluster in ((0, 0), (2, 0), (2, 1)):
             lib.mgt_set_tuning(L.MGT_TUNE_PANEL_REGISTERS, mode)
+            lib.mgt_set_tuning(L.MGT_TUNE_PANEL_CLUSTER, cluster)
             f = E.lu_factor(A.cuda().clone(), check_singular=False)
             outs.append((f.lu.cpu(), f.perm.cpu()))
     finally:
         lib.mgt_set_tuning(L.MGT_TUNE_PANEL_REGISTERS, 1)
+        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_CLUSTER, 1)
         lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, old_rows)
-    assert torch.equal(outs[0][1], outs[1][1])
-    assert torch.equal(outs[0][0], outs[1][0])
+    for o in outs[1:]:
+        assert torch.equal(outs[0][1], o[1])
+        assert torch.equal(outs[0][0], o[0])
     if n == 700:
         assert int(outs[1][1][0]) == 5
     # and the factors are right: P A = L U
