@@ -20,7 +20,14 @@
 namespace mgt {
 
 constexpr int kTB = 64;      // block rows
-constexpr int kTG = 16;      // right-hand-side columns per chain (independent column groups)
+constexpr int kTG = 16;      // right-hand-side columns per chain (independent column groups), narrow
+constexpr int kTGWide = 64;  // wide chains: complex64, large n (more work per loaded block, fewer chains)
+constexpr int kWideMinN = 20000;
+
+// register tile of one thread in a 64 x TG block: TR rows x 4 columns
+template <int TG> struct TriTile;
+template <> struct TriTile<16> { static constexpr int TR = 1, TC = 4, TPR = 4; };    // 64 x 4 threads
+template <> struct TriTile<64> { static constexpr int TR = 4, TC = 4, TPR = 16; };   // 16 x 16 threads
 
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -76,20 +83,29 @@ diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* 
   for (int idx = tid; idx < kTB * kTB; idx += 256) out[idx] = Xs[idx];
 }
 
-// acc (64 x 16, 4 per thread: row tid/4, columns tid%4 + 4b) -= A (64 x 64, smem, padded) * Y (64 x 16, smem)
-template <typename V>
-__device__ __forceinline__ void block_gemm_sub(V (&acc)[4], const V* As, const V* Ys, int tr, int tc) {
-#pragma unroll 8
+// acc (64 x TG, a TR x TC tile per thread: rows TR tr + i, columns tc + TPR j)
+// -= A (64 x 64, smem, padded) * Y (64 x TG, smem)
+template <int TG, typename V>
+__device__ __forceinline__ void block_gemm_sub(V (&acc)[TriTile<TG>::TR][TriTile<TG>::TC], const V* As, const V* Ys,
+                                               int tr, int tc) {
+  constexpr int TR = TriTile<TG>::TR, TC = TriTile<TG>::TC, TPR = TriTile<TG>::TPR;
+#pragma unroll 4
   for (int kk = 0; kk < kTB; ++kk) {
-    const V a = As[tr * (kTB + 1) + kk];
+    V a[TR], y[TC];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) cfms(acc[b], a, Ys[kk * kTG + tc + 4 * b]);
+    for (int i = 0; i < TR; ++i) a[i] = As[(TR * tr + i) * (kTB + 1) + kk];
+#pragma unroll
+    for (int j = 0; j < TC; ++j) y[j] = Ys[kk * TG + tc + TPR * j];
+#pragma unroll
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j) cfms(acc[i][j], a[i], y[j]);
   }
 }
 
 // Persistent solve of one triangle.  Work items (block row, column group) are
 // claimed in dependency order; groups are independent chains.
-template <typename T, bool UPPER>
+template <typename T, bool UPPER, int TG>
 __global__ void __launch_bounds__(256)
 tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
                  cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols, unsigned* counter, unsigned* flags,
@@ -98,13 +114,14 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
   // replay from a CUDA graph never sees the previous run's flags as ready
   const unsigned epoch = *(volatile const unsigned*)epoch_ptr;
   using V = cplx<T>;
+  constexpr int TR = TriTile<TG>::TR, TC = TriTile<TG>::TC, TPR = TriTile<TG>::TPR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* As = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
-  V* Ys = As + kTB * (kTB + 1);                      // [kTB][kTG]
+  V* Ys = As + kTB * (kTB + 1);                      // [kTB][TG]
   __shared__ unsigned s_item;
   __shared__ int s_fail;
-  const int tid = threadIdx.x, tr = tid >> 2, tc = tid & 3;
-  const int nb = (n + kTB - 1) / kTB, ng = (ncols + kTG - 1) / kTG;
+  const int tid = threadIdx.x, tr = tid / TPR, tc = tid % TPR;
+  const int nb = (n + kTB - 1) / kTB, ng = (ncols + TG - 1) / TG;
   const unsigned items = (unsigned)nb * ng;
   while (true) {
     if (tid == 0) { s_item = atomicAdd(counter, 1u); s_fail = 0; }
@@ -113,14 +130,16 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
     if (k >= items) break;
     const int kr = (int)(k / ng), g = (int)(k % ng);
     const int i = UPPER ? nb - 1 - kr : kr;
-    const int r0 = i * kTB, rb = min(kTB, n - r0), cg = g * kTG;
+    const int r0 = i * kTB, rb = min(kTB, n - r0), cg = g * TG;
     unsigned* gflags = flags + (size_t)g * nb;
-    V acc[4];
+    V acc[TR][TC];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int c = cg + tc + 4 * b;
-      acc[b] = (tr < rb && c < ncols) ? X[(int64_t)(r0 + tr) * ldx + c] : czero<V>();
-    }
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TC; ++b) {
+        const int r = TR * tr + a, c = cg + tc + TPR * b;
+        acc[a][b] = (r < rb && c < ncols) ? X[(int64_t)(r0 + r) * ldx + c] : czero<V>();
+      }
     // dependencies in completion order: ascending for L, descending for U
     const int ndep = UPPER ? nb - 1 - i : i;
     for (int d = 0; d < ndep; ++d) {
@@ -140,12 +159,12 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       }
       __syncthreads();
       if (s_fail) return;
-      for (int idx = tid; idx < kTB * kTG; idx += 256) {
-        int r = idx >> 4, c = idx & 15;
+      for (int idx = tid; idx < kTB * TG; idx += 256) {
+        int r = idx / TG, c = idx % TG;
         Ys[idx] = (r < cb && cg + c < ncols) ? ldcg(X + (int64_t)(c0 + r) * ldx + cg + c) : czero<V>();
       }
       __syncthreads();
-      block_gemm_sub(acc, As, Ys, tr, tc);
+      block_gemm_sub<TG>(acc, As, Ys, tr, tc);
       __syncthreads();
     }
     // X_i = Inv_i * acc
@@ -155,22 +174,28 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       As[r * (kTB + 1) + c] = inv[idx];
     }
 #pragma unroll
-    for (int b = 0; b < 4; ++b) Ys[tr * kTG + tc + 4 * b] = acc[b];
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TC; ++b) Ys[(TR * tr + a) * TG + tc + TPR * b] = acc[a][b];
     __syncthreads();
-    V out[4];
+    V out[TR][TC];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) out[b] = czero<V>();
-    block_gemm_sub(out, As, Ys, tr, tc);   // out = -Inv * acc
+    for (int a = 0; a < TR; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int c = cg + tc + 4 * b;
-      if (tr < rb && c < ncols) {
-        V v = out[b];
-        v.x = -v.x;
-        v.y = -v.y;
-        X[(int64_t)(r0 + tr) * ldx + c] = v;
+      for (int b = 0; b < TC; ++b) out[a][b] = czero<V>();
+    block_gemm_sub<TG>(out, As, Ys, tr, tc);   // out = -Inv * acc
+#pragma unroll
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TC; ++b) {
+        const int r = TR * tr + a, c = cg + tc + TPR * b;
+        if (r < rb && c < ncols) {
+          V v = out[a][b];
+          v.x = -v.x;
+          v.y = -v.y;
+          X[(int64_t)(r0 + r) * ldx + c] = v;
+        }
       }
-    }
     __threadfence();
     __syncthreads();
     if (tid == 0) st_release_u32(gflags + i, epoch);
@@ -212,14 +237,23 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   using V = cplx<T>;
   const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
   const size_t smem = (size_t)(kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
-  static int max_ctas = 0;
+  const size_t smem_w = (size_t)(kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
+  static int max_ctas = 0, max_ctas_w = 0;
   static std::once_flag once;
-  std::call_once(once, [smem, smem_inv] {
+  std::call_once(once, [smem, smem_w, smem_inv] {
     cudaFuncSetAttribute(diag_inverse_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
-    cudaFuncSetAttribute(tri_solve_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    max_ctas = resident_ctas((const void*)tri_solve_kernel<T, UPPER>, smem);
+    cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    max_ctas = resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTG>, smem);
+    if constexpr (sizeof(T) == 4) {
+      cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTGWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_w);
+      max_ctas_w = resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTGWide>, smem_w);
+    }
   });
-  const int nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG;
+  // wide column groups where block rows alone give enough parallelism
+  const bool wide = sizeof(T) == 4 && n >= kWideMinN;
+  const int tg = wide ? kTGWide : kTG;
+  const int nb = (n + kTB - 1) / kTB, ng = (nrhs + tg - 1) / tg;
   unsigned* counter = (unsigned*)work;
   unsigned* flags = (unsigned*)((char*)work + 256);
   size_t flag_bytes = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
@@ -230,8 +264,19 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   count_launch();
   tri_start_kernel<<<std::max(1, std::min(nb * ng, 1 << 16) / 256 + 1), 256, 0, s>>>(counter, epoch, flags, nb * ng);
   count_launch();
-  const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
-  tri_solve_kernel<T, UPPER><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch, status);
+  if constexpr (sizeof(T) == 4) {
+    if (wide) {
+      const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas_w);
+      tri_solve_kernel<T, UPPER, kTGWide><<<grid, 256, smem_w, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags,
+                                                                     epoch, status);
+      return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+    }
+  }
+  {
+    const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
+    tri_solve_kernel<T, UPPER, kTG><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch,
+                                                             status);
+  }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 

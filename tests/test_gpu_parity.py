@@ -298,6 +298,23 @@ def test_lu_solve_any_workspace_contents(dtype, fill):
     assert rel(X.cpu().to(torch.complex128), ref) < (1e-12 if dtype == torch.complex128 else 1e-4)
 
 
+@pytest.mark.gpu
+def test_lu_solve_wide_column_groups():
+    """complex64 systems of order >= 20000 solve in 64-column chains (fewer,
+    wider work items); the result must be as good as the narrow chains'."""
+    from magreete_gb300 import engine as E
+    n, R = 20480, 40
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    A = (torch.randn(n, n, dtype=torch.complex64, device="cuda", generator=gen) +
+         (4 * n ** 0.5) * torch.eye(n, dtype=torch.complex64, device="cuda"))
+    B = torch.randn(n, R, dtype=torch.complex64, device="cuda", generator=gen)
+    f = E.lu_factor(A.clone())
+    X = E.lu_solve(f, B)
+    r = torch.linalg.norm(A @ X - B) / (torch.linalg.norm(A) * torch.linalg.norm(X))
+    assert r.item() < 1e-6, r.item()
+    del A, f
+
+
 def test_singular_matrix_raises():
     from magreete_gb300 import engine as E
     A = torch.randn(80, 80, dtype=torch.complex128)
