@@ -261,6 +261,9 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *                        CTAs (8 where the device schedules no larger cluster)
  *                        run as one thread-block cluster and exchange pivots
  *                        through distributed shared memory; 0: through L2
+ *   MGT_TUNE_SYM_ASSEMBLY 1 (default): mgt_assemble_system evaluates each pair
+ *                        of points once and writes both mirror-image blocks
+ *                        (bitwise the same matrix); 0: every block evaluated
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -272,6 +275,7 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_LOOKAHEAD 7
 #define MGT_TUNE_FUSED_RIGHT 8
 #define MGT_TUNE_PANEL_CLUSTER 9
+#define MGT_TUNE_SYM_ASSEMBLY 10
 #define MGT_TC_TF32X3 0
 #define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);

@@ -31,6 +31,7 @@ MGT_TUNE_TC_PRECISION = 6
 MGT_TUNE_LOOKAHEAD = 7
 MGT_TUNE_FUSED_RIGHT = 8
 MGT_TUNE_PANEL_CLUSTER = 9
+MGT_TUNE_SYM_ASSEMBLY = 10
 MGT_TC_TF32X3, MGT_TC_F16X2 = 0, 1
 
 _vp = ctypes.c_void_p

@@ -6,6 +6,8 @@
 // 32*d*16 bytes.  The kernel is store-bandwidth bound for the 3D kinds and
 // FP64-pipe bound (Bessel J0/Y0/J1/Y1) for the 2D kinds.
 // The Green's blocks themselves are in green.cuh.
+#include <atomic>
+
 #include "common.cuh"
 #include "df.cuh"
 #include "green.cuh"
@@ -80,6 +82,82 @@ assemble_system_kernel(const double* __restrict__ pts, int n, double k0, double2
   }
 }
 
+// The same matrix from half the Green's blocks: G(-r) = G(r) and every block
+// is symmetric, so M is complex-symmetric.  One CTA per 16 x 16 tile of point
+// pairs with bj >= bi evaluates each pair once (FP64, into shared memory)
+// and writes the tile and, off the diagonal, its mirror image, both as
+// contiguous row segments.  Negating r changes neither |r| nor the products
+// of its components, so the mirrored values are bitwise those of the lower
+// triangle evaluated directly.
+constexpr int kSymTP = 16;
+
+template <int KIND>
+__global__ void __launch_bounds__(kSymTP * kSymTP)
+assemble_system_sym_kernel(const double* __restrict__ pts, int n, double k0, double2 coef, double2 diag,
+                           OutSpec o1, OutSpec o2) {
+  constexpr int dim = Kind<KIND>::dim, d = Kind<KIND>::d;
+  constexpr int TP = kSymTP, W = TP * d;          // tile side in matrix rows / columns
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi) return;
+  extern __shared__ __align__(16) unsigned char asm_smem[];
+  double2* S = reinterpret_cast<double2*>(asm_smem);   // [TP][TP][d * d]
+  const int tid = threadIdx.x, p = tid / TP, q = tid % TP;
+  const int i = bi * TP + p, j = bj * TP + q;
+  double2 g[d * d];
+  if (i < n && j < n) {
+    if (i == j) {
+#pragma unroll
+      for (int a = 0; a < d; ++a)
+#pragma unroll
+        for (int b = 0; b < d; ++b) g[a * d + b] = (a == b) ? diag : make_double2(0.0, 0.0);
+    } else {
+      double r[dim];
+#pragma unroll
+      for (int c = 0; c < dim; ++c) r[c] = pts[(int64_t)i * dim + c] - pts[(int64_t)j * dim + c];
+      if (!green_block<KIND>(r, k0, false, 0.0, g)) {
+#pragma unroll
+        for (int e = 0; e < d * d; ++e)
+          g[e] = make_double2(__longlong_as_double(0x7ff8000000000000ll), __longlong_as_double(0x7ff8000000000000ll));
+      } else {
+#pragma unroll
+        for (int e = 0; e < d * d; ++e) {
+          double2 v = g[e];
+          g[e] = make_double2(-(coef.x * v.x - coef.y * v.y), -(coef.x * v.y + coef.y * v.x));
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < d * d; ++e) g[e] = make_double2(0.0, 0.0);
+  }
+#pragma unroll
+  for (int e = 0; e < d * d; ++e) S[(p * TP + q) * d * d + e] = g[e];
+  __syncthreads();
+  // tile (bi, bj): row i d + a, column j d + b
+  for (int idx = tid; idx < W * W; idx += TP * TP) {
+    const int rr = idx / W, cc = idx - rr * W;
+    const int pp = rr / d, a = rr - pp * d, qq = cc / d, b = cc - qq * d;
+    const int ii = bi * TP + pp, jj = bj * TP + qq;
+    if (ii < n && jj < n) {
+      const double2 v = S[(pp * TP + qq) * d * d + a * d + b];
+      store_entry(o1, (int64_t)ii * d + a, (int64_t)jj * d + b, v);
+      store_entry(o2, (int64_t)ii * d + a, (int64_t)jj * d + b, v);
+    }
+  }
+  if (bi == bj) return;
+  // mirror tile (bj, bi): row j d + b, column i d + a holds the same value
+  for (int idx = tid; idx < W * W; idx += TP * TP) {
+    const int rr = idx / W, cc = idx - rr * W;
+    const int qq = rr / d, b = rr - qq * d, pp = cc / d, a = cc - pp * d;
+    const int ii = bi * TP + pp, jj = bj * TP + qq;
+    if (ii < n && jj < n) {
+      const double2 v = S[(pp * TP + qq) * d * d + a * d + b];
+      store_entry(o1, (int64_t)jj * d + b, (int64_t)ii * d + a, v);
+      store_entry(o2, (int64_t)jj * d + b, (int64_t)ii * d + a, v);
+    }
+  }
+}
+
 // Propagator: coef * G(t_i - s_j).  Threads run over the output's column
 // points: sources (normal) or targets (transposed output).
 template <int KIND, bool TRANSPOSE>
@@ -130,14 +208,32 @@ assemble_propagator_kernel(const double* __restrict__ tgt, int nt, const double*
   }
 }
 
+static std::atomic<int> g_sym_assembly{1};   // assemble from half the Green's blocks
+
 template <int KIND>
 static cudaError_t launch_system(const double* pts, int n, double k0, double2 coef, double2 diag,
                                  OutSpec o1, OutSpec o2, cudaStream_t s) {
+  if (g_sym_assembly.load(std::memory_order_relaxed)) {
+    constexpr int d = Kind<KIND>::d;
+    const int nb = (n + kSymTP - 1) / kSymTP;
+    if (nb <= 65535) {
+      const size_t smem = (size_t)kSymTP * kSymTP * d * d * sizeof(double2);
+      assemble_system_sym_kernel<KIND><<<dim3(nb, nb), kSymTP * kSymTP, smem, s>>>(pts, n, k0, coef, diag, o1, o2);
+      count_launch();
+      return cudaGetLastError();
+    }
+  }
   dim3 grid((n + kAsmThreads - 1) / kAsmThreads, (n + kAsmRows - 1) / kAsmRows);
   assemble_system_kernel<KIND><<<grid, kAsmThreads, 0, s>>>(pts, n, k0, coef, diag, o1, o2);
   count_launch();
   return cudaGetLastError();
 }
+
+int set_sym_assembly(int v) {
+  g_sym_assembly.store(v ? 1 : 0);
+  return MGT_OK;
+}
+int get_sym_assembly() { return g_sym_assembly.load(); }
 
 template <int KIND>
 static cudaError_t launch_prop(const double* t, int nt, const double* src, int ns, double k0,

@@ -1245,6 +1245,9 @@ static int cluster_panel_max() {
   return cmax;
 }
 
+int set_sym_assembly(int v);
+int get_sym_assembly();
+
 // Per-thread side stream and fork / join events for the lookahead update.
 struct SideStream {
   cudaStream_t s = nullptr;
@@ -1814,6 +1817,7 @@ extern "C" int mgt_set_tuning(int key, int value) {
     g_panel_cluster.store(value ? 1 : 0);
     return MGT_OK;
   }
+  if (key == MGT_TUNE_SYM_ASSEMBLY) return set_sym_assembly(value);
   return MGT_ERR_ARG;
 }
 
@@ -1827,5 +1831,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_LOOKAHEAD) return g_lookahead.load();
   if (key == MGT_TUNE_FUSED_RIGHT) return g_fused_right.load();
   if (key == MGT_TUNE_PANEL_CLUSTER) return g_panel_cluster.load();
+  if (key == MGT_TUNE_SYM_ASSEMBLY) return get_sym_assembly();
   return MGT_ERR_ARG;
 }
