@@ -495,8 +495,7 @@ def run_sweep(args):
     _lib.load()
     probs = W.sweep_2d(args.sweep)
     groups = [probs[i:i + args.group] for i in range(0, len(probs), args.group)]
-    best = batch.autotune(groups[0], cache=os.path.join(ROOT, "gpurun_out", "tuning.json")
-                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else batch.TUNE_CACHE)
+    best = batch.autotune(groups[0])
     t_total, worst, extra_total, flops = 0.0, 0.0, 0, 0.0
     for g in groups:
         sw = batch.BatchedSweep(g, branches=best["branches"])
