@@ -267,6 +267,68 @@ def e2e_window(problems, precision):
     return h2d, d2h
 
 
+def secondary_rooflines():
+    """The other two kernels with large shares of the stream, timed alone with
+    CUDA events after the timed region: the double-float residual (FP32 pipe;
+    3D N=4000, n = 12000, 64 right-hand sides) and the LU panel (latency: one
+    cross-CTA exchange per column; the complex64 LU of 2D N=1000, n = 2000,
+    where the trailing update is negligible)."""
+    from magreete_gb300 import engine as E, selfterm
+    from magreete_gb300 import workloads as W
+    dev = torch.device("cuda")
+    out = {}
+    prob = W.cfg2()
+    pts = prob.points.to(dev)
+    coef = prob.alpha * prob.k0 ** 2
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    (Mdf,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf",))
+    n, R = prob.n, prob.nrhs
+    X = torch.randn(n, R, dtype=torch.complex128, device=dev)
+    B = torch.randn(n, R, dtype=torch.complex128, device=dev)
+    E.residual(Mdf, X, B)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        E.residual(Mdf, X, B)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 3
+    macs = float(n) * n * R
+    ops = 52.0 * macs          # FP32 operations of one double-float complex multiply-add
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk = 2.07e9
+    peak = sms * 128 * clk      # FP32 lane-operations per second (nominal: 128 lanes per SM, max clock)
+    out["residual_df"] = {"bound": "fp32 pipe", "n": n, "nrhs": R, "ms": ms,
+                          "complex_macs_per_s": macs / (ms * 1e-3),
+                          "fp32_ops_per_s": ops / (ms * 1e-3), "peak_fp32_ops_per_s": peak,
+                          "frac": ops / (ms * 1e-3) / peak,
+                          "peak_source": "nominal: SMs x 128 FP32 lanes x 2.07 GHz; ~52 FP32 operations per "
+                                         "double-float complex multiply-add"}
+    del Mdf
+    prob = W.cfg1()
+    pts = prob.points.to(dev)
+    coef = prob.alpha * prob.k0 ** 2
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    (M32,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("c64",))
+    ts = []
+    for rep in range(4):
+        A = torch.empty_strided(M32.size(), M32.stride(), dtype=M32.dtype, device=dev)
+        A.copy_(M32)
+        torch.cuda.synchronize()
+        e0.record()
+        E.lu_factor(A, check_singular=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    lu_ms = min(ts[1:])
+    out["lu_panel"] = {"bound": "latency (one cross-CTA pivot exchange per column)", "n": prob.n,
+                       "lu_ms": lu_ms, "us_per_column": 1e3 * lu_ms / prob.n,
+                       "note": "complex64 LU of order 2000: panels in one thread-block cluster; the "
+                               "trailing update is under 10% of it"}
+    return out
+
+
 def run_ours(args, rank, world, local):
     import magreete_gb300  # noqa: F401
     from magreete_gb300 import _lib
@@ -364,6 +426,7 @@ def run_ours(args, rank, world, local):
                                f"bf16_tflops of {src} peaks",
                 "measured": "CUDA events around each launch on its stream, sequential pass over the first timed window",
                 "in_mix_tflops": (mix_flops / (mix_ms * 1e-3) / 1e12) if mix_ms > 0 else None}
+    secondary = secondary_rooflines() if rank == 0 else None
     cpu = None
     if world == 1:
         timed = [p for w in wins[args.warmup:] for p in w]
@@ -379,7 +442,8 @@ def run_ours(args, rank, world, local):
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (matrices 24 n^2 bytes)"},
             "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
             "refinement": {"max_iterations": max(iters), "max_rel_residual": max(rres)},
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+            "e2e": e2e, "roofline": roofline, "roofline_other": secondary, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": launches}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
