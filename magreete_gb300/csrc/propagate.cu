@@ -209,7 +209,7 @@ int assemble_propagator_into(int kind, const double* t, int nt, const double* sr
 int residual_rect(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B, int64_t ldb,
                   double2* R, int64_t ldr, int rows, int kdim, int nrhs, cudaStream_t s, double2* partial,
                   int64_t partial_elems);
-int residual_ksplit(int rows, int kdim);
+int64_t residual_partial_elems(int64_t rows, int64_t kdim, int64_t nrhs);
 int split_df(const double2* X, int64_t ldx, float4* Xs, int64_t ldy, int n, int ncols, cudaStream_t s);
 
 // Double-float path: the propagator's detector rows are assembled in chunks
@@ -228,8 +228,7 @@ static size_t prop_chunk_bytes(int64_t nt, int64_t ns, int d) {
   return ((size_t)prop_chunk_targets(nt, ns, d) * d * d * ns * sizeof(float4) + 255) & ~size_t(255);
 }
 static size_t prop_part_elems(int64_t nt, int64_t ns, int64_t nrhs, int d) {
-  const int64_t ct = prop_chunk_targets(nt, ns, d);
-  return (size_t)residual_ksplit((int)(ct * d), (int)(d * ns)) * ct * d * std::min<int64_t>(nrhs, 128);
+  return (size_t)residual_partial_elems(prop_chunk_targets(nt, ns, d) * d, (int64_t)d * ns, nrhs);
 }
 static size_t prop_df_bytes(int64_t nt, int64_t ns, int64_t nrhs, int d) {
   return prop_xs_bytes(ns, nrhs, d) + prop_chunk_bytes(nt, ns, d) + prop_part_elems(nt, ns, nrhs, d) * sizeof(double2);

@@ -15,22 +15,28 @@
 
 namespace mgt {
 
-constexpr int kResRows = 32;   // rows of R per CTA
-constexpr int kResK = 16;      // K chunk staged in shared memory
+constexpr int kResRPT = 2;              // rows of R per thread
+constexpr int kResRows = 16 * kResRPT;  // rows of R per CTA
+constexpr int kResK = 16;               // K chunk staged in shared memory
+// Columns of R per launch.  Two 94-register CTAs of 64 columns per SM beat
+// one 156-register CTA of 128 columns once K is split (GB300, n = 12000,
+// 128 right-hand sides: 29.9 vs 31.1 ms).
+constexpr int kResCols = 64;
 
-// Each thread owns rows {ty, ty+16} and columns {tx + 16 j : j < RT}.
+// Each thread owns rows {ty + 16 i : i < kResRPT} and columns {tx + 16 j : j < RT}.
 template <int RT>
 __global__ void __launch_bounds__(256)
 residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __restrict__ Xs, int64_t ldxs,
                    const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R, int64_t ldr, int n,
                    int kdim, int ncols, int col_base, int k_per_split, double2* __restrict__ partial) {
+  constexpr int RPT = kResRPT;
   __shared__ float4 Ms[kResRows][kResK + 1];
   __shared__ float4 Xsh[kResK][16 * RT];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int row0 = blockIdx.x * kResRows;
-  float4 acc[2][RT];
+  float4 acc[RPT][RT];
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < RPT; ++i)
 #pragma unroll
     for (int j = 0; j < RT; ++j) acc[i][j] = make_float4(0.f, 0.f, 0.f, 0.f);
   // split-K (partial != null): this CTA covers K range [kbeg, kend) and
@@ -38,7 +44,7 @@ residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __re
   const int kbeg = blockIdx.y * k_per_split, kend = min(kdim, kbeg + k_per_split);
   for (int k0 = kbeg; k0 < kend; k0 += kResK) {
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < RPT; ++q) {
       int idx = tid + 256 * q;
       int r = idx >> 4, kk = idx & 15;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -52,20 +58,22 @@ residual_df_kernel(const float4* __restrict__ M, int64_t ldm, const float4* __re
       Xsh[kk][c] = v;
     }
     __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
     for (int kk = 0; kk < kResK; ++kk) {
-      float4 a0 = Ms[ty][kk], a1 = Ms[ty + 16][kk];
+      float4 a[RPT];
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) a[i] = Ms[ty + 16 * i][kk];
 #pragma unroll
       for (int j = 0; j < RT; ++j) {
-        float4 x = Xsh[kk][tx + 16 * j];
-        df_cmac(acc[0][j], a0, x);
-        df_cmac(acc[1][j], a1, x);
+        const float4 x = Xsh[kk][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) df_cmac(acc[i][j], a[i], x);
       }
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < RPT; ++i) {
     int r = row0 + ty + 16 * i;
     if (r >= n) continue;
 #pragma unroll
@@ -145,6 +153,21 @@ static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int6
                                               partial);
 }
 
+// resident CTAs per SM of residual_df_kernel<RT> (1 when no device answers)
+template <int RT>
+static int residual_occupancy() {
+  static int occ = 1;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, residual_df_kernel<RT>, 256, 0) == cudaSuccess && b > 0)
+      occ = b;
+    else
+      cudaGetLastError();
+  });
+  return occ;
+}
+
 // R = B - sum of the split-K partials (FP64)
 __global__ void residual_reduce_kernel(const double2* __restrict__ partial, int ksplit, int n, int ncols,
                                        const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R,
@@ -173,36 +196,62 @@ static int res_num_sms() {
   return sms;
 }
 
-// K splits for a rows x kdim residual: enough CTAs for two waves when the
-// rows alone give fewer, at least 1024 columns of K per split
-int residual_ksplit(int rows, int kdim) {
-  const int rb = (rows + kResRows - 1) / kResRows;
-  const int want = (2 * res_num_sms() + rb - 1) / rb;
-  return std::max(1, std::min({want, kdim / 1024, 32}));
+// K splits of a rows x kdim residual over ncols (<= kResCols) columns.
+// Many short CTAs balance the SMs better than a few long ones: the split
+// aims for at least six waves of CTAs, then takes the first split whose last
+// wave is at least 97% full (else the fullest), at most 16 splits of at
+// least 256 columns of K each.  Measured on GB300 (64 columns): n = 2000
+// 1.12 -> 0.47 ms, 12000 19.5 -> 15.5 ms, 27000 81.6 -> 75 ms.
+int residual_ksplit(int rows, int kdim, int ncols) {
+  if (rows <= 0 || kdim <= 0) return 1;
+  const int nc = std::min(std::max(ncols, 1), kResCols);
+  const int occ = nc <= 16 ? residual_occupancy<1>() : nc <= 32 ? residual_occupancy<2>() : residual_occupancy<4>();
+  const int64_t slots = (int64_t)res_num_sms() * occ;
+  const int64_t rb = (rows + kResRows - 1) / kResRows;
+  const int kmax = std::max(1, std::min(16, kdim / 256));
+  const int lo = (int)std::min<int64_t>(kmax, std::max<int64_t>(1, (6 * slots + rb - 1) / rb));
+  int best = lo;
+  double best_fill = 0.0;
+  for (int ks = lo; ks <= kmax; ++ks) {
+    const int64_t ctas = rb * ks, waves = (ctas + slots - 1) / slots;
+    const double fill = (double)ctas / (double)(waves * slots);
+    if (fill >= 0.97) return ks;
+    if (fill > best_fill) { best_fill = fill; best = ks; }
+  }
+  return best;
+}
+
+// complex128 elements of the split-K partial buffer for a rows x kdim residual
+// with nrhs right-hand sides
+int64_t residual_partial_elems(int64_t rows, int64_t kdim, int64_t nrhs) {
+  if (rows <= 0 || kdim <= 0 || nrhs <= 0 || rows > (1 << 30) || kdim > (1 << 30)) return 0;
+  const int nc = (int)std::min<int64_t>(nrhs, kResCols);
+  const int ks = residual_ksplit((int)rows, (int)kdim, nc);
+  return ks > 1 ? (int64_t)ks * rows * nc : 0;
 }
 
 // R (rows x nrhs) = B - M Xs, M (rows x kdim) double-float, Xs (kdim x nrhs,
 // leading dimension ldxs) the double-float copy of X; B may be null (zero).
-// With a partial buffer (partial_elems complex128) the K range is split
-// across CTAs (short, wide M): residual_ksplit(rows, kdim) splits, fewer if
-// the buffer holds fewer than splits x rows x min(nrhs, 128).
+// Columns go in tiles of kResCols.  With a partial buffer (partial_elems
+// complex128) the K range is split across CTAs: residual_ksplit splits,
+// fewer if the buffer holds fewer than splits x rows x min(nrhs, kResCols).
 int residual_rect(const float4* M, int64_t ldm, const float4* Xs, int64_t ldxs, const double2* B, int64_t ldb,
                   double2* R, int64_t ldr, int rows, int kdim, int nrhs, cudaStream_t s, double2* partial,
                   int64_t partial_elems) {
-  int ksplit = partial ? residual_ksplit(rows, kdim) : 1;
+  const int ncmax = std::min(nrhs, kResCols);
+  int ksplit = partial ? residual_ksplit(rows, kdim, ncmax) : 1;
   // never more splits than the partial buffer holds
-  const int64_t per_split = (int64_t)rows * std::min(nrhs, 128);
+  const int64_t per_split = (int64_t)rows * ncmax;
   if (per_split > 0) ksplit = (int)std::max<int64_t>(1, std::min<int64_t>(ksplit, partial_elems / per_split));
   const int kps = ksplit > 1 ? (((kdim + ksplit - 1) / ksplit + kResK - 1) / kResK) * kResK : kdim;
   double2* part = ksplit > 1 ? partial : nullptr;
-  for (int c0 = 0; c0 < nrhs; c0 += 128) {
-    int nc = std::min(128, nrhs - c0);
+  for (int c0 = 0; c0 < nrhs; c0 += kResCols) {
+    int nc = std::min(kResCols, nrhs - c0);
     int rt = (nc + 15) / 16;
     switch (rt) {
       case 1: launch_residual<1>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
       case 2: launch_residual<2>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
-      case 3: case 4: launch_residual<4>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
-      default: launch_residual<8>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
+      default: launch_residual<4>(M, ldm, Xs, ldxs, B, ldb, R, ldr, rows, kdim, nc, c0, ksplit, kps, part, s); break;
     }
     if (part) {
       const int64_t tot = (int64_t)rows * nc;
@@ -224,10 +273,11 @@ int split_df(const double2* X, int64_t ldx, float4* Xs, int64_t ldy, int n, int 
 }
 
 static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb,
-                         double2* R, int64_t ldr, int n, int nrhs, float4* Xs, cudaStream_t s) {
+                         double2* R, int64_t ldr, int n, int nrhs, float4* Xs, double2* part, int64_t part_elems,
+                         cudaStream_t s) {
   int e = split_df(X, ldx, Xs, nrhs, n, nrhs, s);
   if (e != MGT_OK) return e;
-  return residual_rect(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, n, nrhs, s, nullptr, 0);
+  return residual_rect(M, ldm, Xs, nrhs, B, ldb, R, ldr, n, n, nrhs, s, part, part_elems);
 }
 
 size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem);
@@ -240,6 +290,8 @@ struct RefineWs {
   float2* D32;    // n x nrhs complex64 correction
   double* norms;  // [0] = ||B||^2, [1] = ||R||^2
   void* tri;      // triangular-solve flags
+  double2* part;  // split-K partial sums of the residual
+  int64_t part_elems;
   size_t total;
   RefineWs(void* base, int64_t n, int64_t r) {
     char* b = (char*)base;
@@ -251,6 +303,8 @@ struct RefineWs {
     D32 = (float2*)take(n * r * sizeof(float2));
     norms = (double*)take(2 * sizeof(double));
     tri = take(tri_solve_workspace_bytes(n, r, sizeof(float2)));
+    part_elems = residual_partial_elems(n, n, r);
+    part = (double2*)take(part_elems * sizeof(double2));
     total = off;
   }
 };
@@ -265,7 +319,8 @@ extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, c
 
 extern "C" int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {
   if (!bytes || n <= 0 || nrhs <= 0) return MGT_ERR_ARG;
-  *bytes = (size_t)n * nrhs * sizeof(float4) + 256;
+  *bytes = (((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255)) +
+           residual_partial_elems(n, n, nrhs) * sizeof(double2) + 256;
   return MGT_OK;
 }
 
@@ -275,8 +330,16 @@ extern "C" int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X
   if (!M || !X || !B || !R || !work || n <= 0 || nrhs <= 0 || ldm < n || ldx < nrhs || ldb < nrhs || ldr < nrhs)
     return MGT_ERR_ARG;
   if (n > (1 << 30) || work_bytes < (size_t)n * nrhs * sizeof(float4)) return MGT_ERR_WORKSPACE;
+  // split-K partials after the double-float copy of X, as far as the workspace holds them
+  const size_t xs_bytes = ((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255);
+  double2* part = nullptr;
+  int64_t part_elems = 0;
+  if (work_bytes > xs_bytes) {
+    part = (double2*)((char*)work + xs_bytes);
+    part_elems = (int64_t)((work_bytes - xs_bytes) / sizeof(double2));
+  }
   return residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, (double2*)R, ldr,
-                       (int)n, (int)nrhs, (float4*)work, (cudaStream_t)stream);
+                       (int)n, (int)nrhs, (float4*)work, part, part_elems, (cudaStream_t)stream);
 }
 
 extern "C" int mgt_refine_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {
@@ -315,7 +378,7 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   double prev = 0.0, rel = 0.0;
   int it = 0;
   for (;; ++it) {
-    e = residual_impl((const float4*)M, ldm, Xd, ldx, Bd, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+    e = residual_impl((const float4*)M, ldm, Xd, ldx, Bd, ldb, w.Rr, nr, nn, nr, w.Xs, w.part, w.part_elems, s);
     if (e != MGT_OK) return e;
     if (cudaMemsetAsync(w.norms + 1, 0, sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
     count_launch();
@@ -404,7 +467,8 @@ extern "C" int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, in
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const unsigned eg = (unsigned)((n * nrhs + 255) / 256);
-  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs,
+                        w.part, w.part_elems, s);
   if (e != MGT_OK) return e;
   count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
@@ -426,7 +490,8 @@ extern "C" int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const voi
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const int64_t tot = n * nrhs;
-  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs, s);
+  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs,
+                        w.part, w.part_elems, s);
   if (e != MGT_OK) return e;
   if (cudaMemsetAsync(norms_dev, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
   count_launch(2);

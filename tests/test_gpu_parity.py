@@ -299,6 +299,38 @@ def test_lu_solve_any_workspace_contents(dtype, fill):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("R", [5, 64, 100])
+def test_residual_split_k(R):
+    """Double-float residual B - M X with K split across CTAs (the queried
+    workspace) and unsplit (a workspace holding only the double-float copy
+    of X), for one column tile of 16, one of 64, and tiles of 64 + 36
+    columns.  Bound: n 2^-48 of |M||X| (the low parts are summed in FP32
+    over n terms; observed ~2e-12 at n = 3000)."""
+    import ctypes
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    lib = L.load()
+    gen = torch.Generator().manual_seed(11)
+    N = 1500
+    pts = (torch.rand(N, 2, dtype=torch.float64, generator=gen) * 30.0).cuda()
+    M, Mdf = E.assemble_system("2d_vector", pts, 2.0, 0.3 + 0.2j, 0.1 - 0.05j, ("c128", "cdf"))
+    n = M.shape[0]
+    X = torch.randn(n, R, dtype=torch.complex128, generator=gen).cuda()
+    B = torch.randn(n, R, dtype=torch.complex128, generator=gen).cuda()
+    ref = B - M @ X
+    scale = (M.abs() @ X.abs()).max().item()
+    R_split = E.residual(Mdf, X, B)
+    work = torch.empty(n * R * 16, dtype=torch.uint8, device="cuda")
+    R_one = torch.empty_like(B)
+    L.check(lib.mgt_residual(ctypes.c_void_p(Mdf.data_ptr()), n, n, ctypes.c_void_p(X.data_ptr()), R,
+                             ctypes.c_void_p(B.data_ptr()), R, ctypes.c_void_p(R_one.data_ptr()), R, R,
+                             ctypes.c_void_p(work.data_ptr()), work.numel(),
+                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    for got in (R_split, R_one):
+        assert (got - ref).abs().max().item() <= n * 2.0 ** -48 * scale
+
+
+@pytest.mark.gpu
 def test_lu_solve_wide_column_groups():
     """complex64 systems of order >= 20000 solve in 64-column chains (fewer,
     wider work items); the result must be as good as the narrow chains'."""
