@@ -38,6 +38,27 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+// One element (8 or 16 bytes) copied global -> shared without passing through
+// registers (sm_80 cp.async); zero-filled, with nothing read, when !ok.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const int sz = ok ? BYTES : 0;
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"(BYTES), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Factor blocks staged per CTA: two (the next block loads during the current
+// product) for complex64, one for complex128 (shared memory).
+template <typename T> constexpr int tri_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
+
 // Inverse of every 64 x 64 diagonal block of the unit lower (or upper) factor:
 // one CTA per block, identity right-hand sides, substitution in shared memory.
 template <typename T, bool UPPER>
@@ -103,8 +124,33 @@ __device__ __forceinline__ void block_gemm_sub(V (&acc)[TriTile<TG>::TR][TriTile
   }
 }
 
+// Stage st of work item (block row i, ndep dependencies) into buf: for
+// st < ndep the factor block of dependency st (it does not depend on the
+// flag), for st == ndep the inverted diagonal block (full 64 x 64).
+template <bool UPPER, typename V>
+__device__ __forceinline__ void tri_stage(V* buf, int st, int ndep, const V* __restrict__ F, int64_t ldf,
+                                          const V* __restrict__ Inv, int i, int nb, int n, int r0, int rb, int tid) {
+  if (st < ndep) {
+    const int j = UPPER ? nb - 1 - st : st;
+    const int c0 = j * kTB, cb = min(kTB, n - c0);
+    for (int idx = tid; idx < kTB * kTB; idx += 256) {
+      const int r = idx >> 6, c = idx & 63;
+      const bool ok = r < rb && c < cb;
+      cp_async_elem<(int)sizeof(V)>(buf + r * (kTB + 1) + c, ok ? F + (int64_t)(r0 + r) * ldf + c0 + c : F, ok);
+    }
+  } else {
+    const V* inv = Inv + (int64_t)i * kTB * kTB;
+    for (int idx = tid; idx < kTB * kTB; idx += 256)
+      cp_async_elem<(int)sizeof(V)>(buf + (idx >> 6) * (kTB + 1) + (idx & 63), inv + idx, true);
+  }
+  cp_async_commit();
+}
+
 // Persistent solve of one triangle.  Work items (block row, column group) are
-// claimed in dependency order; groups are independent chains.
+// claimed in dependency order; groups are independent chains.  An item's
+// stages are the factor blocks it depends on, then its inverted diagonal
+// block; each is copied asynchronously, and with two buffers the next stage
+// loads while the current block product runs.
 template <typename T, bool UPPER, int TG>
 __global__ void __launch_bounds__(256)
 tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
@@ -115,9 +161,11 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
   const unsigned epoch = *(volatile const unsigned*)epoch_ptr;
   using V = cplx<T>;
   constexpr int TR = TriTile<TG>::TR, TC = TriTile<TG>::TC, TPR = TriTile<TG>::TPR;
+  constexpr int NBUF = tri_nbuf<T>();
+  constexpr int kAs = kTB * (kTB + 1);               // one padded 64 x 64 block
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  V* As = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
-  V* Ys = As + kTB * (kTB + 1);                      // [kTB][TG]
+  V* Asb = reinterpret_cast<V*>(smem_raw);          // NBUF x [kTB][kTB + 1]
+  V* Ys = Asb + NBUF * kAs;                          // [kTB][TG]
   __shared__ unsigned s_item;
   __shared__ int s_fail;
   const int tid = threadIdx.x, tr = tid / TPR, tc = tid % TPR;
@@ -142,14 +190,12 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       }
     // dependencies in completion order: ascending for L, descending for U
     const int ndep = UPPER ? nb - 1 - i : i;
+    tri_stage<UPPER>(Asb, 0, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
     for (int d = 0; d < ndep; ++d) {
+      const V* As = Asb + (NBUF == 2 ? (d & 1) * kAs : 0);
+      if (NBUF == 2) tri_stage<UPPER>(Asb + ((d + 1) & 1) * kAs, d + 1, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
       const int j = UPPER ? nb - 1 - d : d;
       const int c0 = j * kTB, cb = min(kTB, n - c0);
-      // the block of T does not depend on the flag: load it first
-      for (int idx = tid; idx < kTB * kTB; idx += 256) {
-        int r = idx >> 6, c = idx & 63;
-        As[r * (kTB + 1) + c] = (r < rb && c < cb) ? F[(int64_t)(r0 + r) * ldf + c0 + c] : czero<V>();
-      }
       if (tid == 0) {
         unsigned it = 0;
         while (ld_acquire_u32(gflags + j) != epoch) {
@@ -157,8 +203,12 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
           if (it > 64) __nanosleep(32);
         }
       }
+      if (NBUF == 2) cp_async_wait<1>(); else cp_async_wait<0>();
       __syncthreads();
-      if (s_fail) return;
+      if (s_fail) {
+        cp_async_wait<0>();
+        return;
+      }
       for (int idx = tid; idx < kTB * TG; idx += 256) {
         int r = idx / TG, c = idx % TG;
         Ys[idx] = (r < cb && cg + c < ncols) ? ldcg(X + (int64_t)(c0 + r) * ldx + cg + c) : czero<V>();
@@ -166,13 +216,11 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       __syncthreads();
       block_gemm_sub<TG>(acc, As, Ys, tr, tc);
       __syncthreads();
+      if (NBUF == 1) tri_stage<UPPER>(Asb, d + 1, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
     }
-    // X_i = Inv_i * acc
-    const V* inv = Inv + (int64_t)i * kTB * kTB;
-    for (int idx = tid; idx < kTB * kTB; idx += 256) {
-      int r = idx >> 6, c = idx & 63;
-      As[r * (kTB + 1) + c] = inv[idx];
-    }
+    // X_i = Inv_i * acc, Inv_i in the last stage's buffer
+    const V* As = Asb + (NBUF == 2 ? (ndep & 1) * kAs : 0);
+    cp_async_wait<0>();
 #pragma unroll
     for (int a = 0; a < TR; ++a)
 #pragma unroll
@@ -236,8 +284,8 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
               cudaStream_t s) {
   using V = cplx<T>;
   const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
-  const size_t smem = (size_t)(kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
-  const size_t smem_w = (size_t)(kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
+  const size_t smem = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
+  const size_t smem_w = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
   static int max_ctas = 0, max_ctas_w = 0;
   static std::once_flag once;
   std::call_once(once, [smem, smem_w, smem_inv] {
