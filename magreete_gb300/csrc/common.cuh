@@ -79,6 +79,23 @@ __device__ inline float2 to_c32(double2 v) { return make_float2((float)v.x, (flo
 __device__ inline double2 ldcg(const double2* p) { return __ldcg(p); }
 __device__ inline float2 ldcg(const float2* p) { return __ldcg(p); }
 
+// One element (8 or 16 bytes) copied global -> shared without passing through
+// registers (sm_80 cp.async); zero-filled, with nothing read, when !ok.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const int sz = ok ? BYTES : 0;
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"(BYTES), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Iteration limit of every device-side spin wait (about a few seconds with
 // the back-off below).  A wait that runs out records MGT_ERR_TIMEOUT in the
 // status word and the kernel returns instead of hanging.

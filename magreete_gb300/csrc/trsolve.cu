@@ -38,23 +38,6 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
-// One element (8 or 16 bytes) copied global -> shared without passing through
-// registers (sm_80 cp.async); zero-filled, with nothing read, when !ok.
-template <int BYTES>
-__device__ __forceinline__ void cp_async_elem(void* dst, const void* src, bool ok) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const int sz = ok ? BYTES : 0;
-  if constexpr (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"(BYTES), "r"(sz) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // Factor blocks staged per CTA: two (the next block loads during the current
 // product) for complex64, one for complex128 (shared memory).
 template <typename T> constexpr int tri_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
