@@ -42,15 +42,24 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // product) for complex64, one for complex128 (shared memory).
 template <typename T> constexpr int tri_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
 
+// Row stride of the right-hand sides in diag_inverse_kernel: the four lanes
+// of a column group read rows r..r+3, and a stride of 72 complex64 (an odd
+// multiple of 64 bytes) puts those rows on different banks (with 64 they
+// shared one: 4-way conflicts on every access).
+constexpr int kInvLd = kTB + 8;
+
 // Inverse of every 64 x 64 diagonal block of the unit lower (or upper) factor:
 // one CTA per block, identity right-hand sides, substitution in shared memory.
+// Warp w owns columns 8w..8w+7 of the inverse, which is lower (upper)
+// triangular: the steps above (below) those columns multiply exact zeros and
+// are skipped.
 template <typename T, bool UPPER>
 __global__ void __launch_bounds__(256)
 diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* __restrict__ Inv) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* Ts = reinterpret_cast<V*>(smem_raw);          // [kTB][kTB + 1]
-  V* Xs = Ts + kTB * (kTB + 1);                      // [kTB][kTB]
+  V* Xs = Ts + kTB * (kTB + 1);                      // [kTB][kInvLd]
   __shared__ V dinv[kTB];
   const int tid = threadIdx.x, i = blockIdx.x;
   const int r0 = i * kTB, rb = min(kTB, n - r0);
@@ -59,7 +68,7 @@ diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* 
     Ts[r * (kTB + 1) + c] = (r < rb && c < rb) ? F[(int64_t)(r0 + r) * ldf + r0 + c] : czero<V>();
     V e = czero<V>();
     if (r == c) e.x = 1;
-    Xs[r * kTB + c] = e;
+    Xs[r * kInvLd + c] = e;
   }
   __syncthreads();
   if (UPPER)
@@ -68,23 +77,23 @@ diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* 
   const int warp = tid >> 5, lane = tid & 31;
   const int col = warp * 8 + (lane >> 2), t4 = lane & 3;   // 4 lanes per column, 64 columns
   if (!UPPER) {
-    for (int kk = 0; kk < rb - 1; ++kk) {
+    for (int kk = warp * 8; kk < rb - 1; ++kk) {
       __syncwarp();
-      const V xk = Xs[kk * kTB + col];
-      for (int r = kk + 1 + t4; r < rb; r += 4) cfms(Xs[r * kTB + col], Ts[r * (kTB + 1) + kk], xk);
+      const V xk = Xs[kk * kInvLd + col];
+      for (int r = kk + 1 + t4; r < rb; r += 4) cfms(Xs[r * kInvLd + col], Ts[r * (kTB + 1) + kk], xk);
     }
   } else {
-    for (int kk = rb - 1; kk >= 0; --kk) {
+    for (int kk = min(rb - 1, warp * 8 + 7); kk >= 0; --kk) {
       __syncwarp();
-      if (t4 == 0) Xs[kk * kTB + col] = cmul(Xs[kk * kTB + col], dinv[kk]);
+      if (t4 == 0) Xs[kk * kInvLd + col] = cmul(Xs[kk * kInvLd + col], dinv[kk]);
       __syncwarp();
-      const V xk = Xs[kk * kTB + col];
-      for (int r = t4; r < kk; r += 4) cfms(Xs[r * kTB + col], Ts[r * (kTB + 1) + kk], xk);
+      const V xk = Xs[kk * kInvLd + col];
+      for (int r = t4; r < kk; r += 4) cfms(Xs[r * kInvLd + col], Ts[r * (kTB + 1) + kk], xk);
     }
   }
   __syncthreads();
   V* out = Inv + (int64_t)i * kTB * kTB;
-  for (int idx = tid; idx < kTB * kTB; idx += 256) out[idx] = Xs[idx];
+  for (int idx = tid; idx < kTB * kTB; idx += 256) out[idx] = Xs[(idx >> 6) * kInvLd + (idx & 63)];
 }
 
 // acc (64 x TG, a TR x TC tile per thread: rows TR tr + i, columns tc + TPR j)
@@ -266,7 +275,7 @@ template <typename T, bool UPPER>
 int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int nrhs, void* work, int* status,
               cudaStream_t s) {
   using V = cplx<T>;
-  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
+  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kInvLd) * sizeof(V);
   const size_t smem = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
   const size_t smem_w = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
   static int max_ctas = 0, max_ctas_w = 0;
@@ -317,7 +326,7 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
 template <typename T>
 int lower_block_inverses(const cplx<T>* F, int64_t ldf, int n, cplx<T>* Inv, cudaStream_t s) {
   using V = cplx<T>;
-  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kTB) * sizeof(V);
+  const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kInvLd) * sizeof(V);
   static std::once_flag once;
   std::call_once(once, [smem_inv] {
     cudaFuncSetAttribute(diag_inverse_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
