@@ -157,9 +157,11 @@ int mgt_workspace_status(void* work, int32_t out[2], void* stream);
 /*
  * Residual R = B - M X with M (n x n) in MGT_CDF form, X, B, R complex128
  * (n x nrhs), computed in double-float arithmetic on the FP32 pipes
- * (products exact via fma, sums compensated).  `work` must hold
- * mgt_residual_workspace_bytes(n, nrhs) bytes.  Used by iterative
- * refinement.
+ * (products exact via fma, sums compensated).  `work` must hold at least
+ * n * nrhs * 16 bytes (the double-float copy of X); the
+ * mgt_residual_workspace_bytes(n, nrhs) size adds room for split-K partial
+ * sums, and whatever the workspace holds beyond the copy of X is used for
+ * them (more CTAs over K: fewer idle SMs).  Used by iterative refinement.
  */
 int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
 int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X, int64_t ldx,
