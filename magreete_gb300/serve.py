@@ -105,6 +105,81 @@ def serve_sequential(problems, precision="mixed", device_inputs=None, start=None
     return out
 
 
+class Admission:
+    """Device-memory admission for the server, thread-safe and free of CUDA
+    calls: requests wait in arrival order and the oldest is admitted once its
+    bytes fit the budget next to those in use (no request overtakes an older
+    one that does not fit yet).  Cached objects (factorisations) hold bytes
+    too, least recently used first out: when the cache outgrows its size,
+    and whenever the waiting request would fit without them."""
+
+    def __init__(self, budget):
+        self.budget = int(budget)
+        self.in_use = 0
+        self.cv = threading.Condition()
+        self.queue = collections.deque()
+        self.closed = False
+        self.cache = collections.OrderedDict()     # key -> (object, bytes held)
+
+    def put(self, item, need):
+        """Queue ``item`` needing ``need`` bytes; MemoryError if it can never fit."""
+        if need > self.budget:
+            raise MemoryError(f"request needs {need} B, above the HBM budget of {self.budget} B")
+        with self.cv:
+            self.queue.append((item, need))
+            self.cv.notify_all()
+
+    def take(self):
+        """Block until the oldest request fits, admit it and return (item, need);
+        None once closed and drained."""
+        with self.cv:
+            while True:
+                if self.queue:
+                    need = self.queue[0][1]
+                    # cached objects give way to a waiting request
+                    while self.in_use + need > self.budget and self.cache:
+                        _, (_, held) = self.cache.popitem(last=False)
+                        self.in_use -= held
+                    if self.in_use + need <= self.budget:
+                        self.in_use += need
+                        return self.queue.popleft()
+                elif self.closed:
+                    return None
+                self.cv.wait()
+
+    def release(self, need):
+        with self.cv:
+            self.in_use -= need
+            self.cv.notify_all()
+
+    def cache_get(self, key):
+        with self.cv:
+            hit = self.cache.get(key)
+            if hit is None:
+                return None
+            self.cache.move_to_end(key)
+            return hit[0]
+
+    def cache_put(self, key, obj, held, limit):
+        """Keep ``obj`` (holding ``held`` bytes) under ``key``; at most ``limit``
+        objects stay cached."""
+        with self.cv:
+            old = self.cache.pop(key, None)
+            if old is not None:
+                self.in_use -= old[1]
+            self.cache[key] = (obj, held)
+            self.in_use += held
+            while len(self.cache) > limit:
+                _, (_, h) = self.cache.popitem(last=False)
+                self.in_use -= h
+            self.cv.notify_all()
+
+    def close(self):
+        with self.cv:
+            self.closed = True
+            self.cv.notify_all()
+
+
 class Server:
     """Continuous-batching solve server on one GPU.
 
@@ -113,6 +188,8 @@ class Server:
                  (default: 85% of the free memory at start)
     precision:   "mixed" (default) or "fp64"
     host_results: copy each result to host memory before completing it
+    factor_cache: factorisations kept for re-queries at the same frequency
+                 (they count against the budget and give way to waiting requests)
     """
 
     def __init__(self, slots=4, hbm_budget=None, precision="mixed", host_results=False, factor_cache=0):
@@ -121,14 +198,11 @@ class Server:
         self.device = torch.device("cuda", torch.cuda.current_device())
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
+        self.admission = Admission(self.budget)
         self.precision = precision
         self.host_results = host_results
-        self.in_use = 0
-        self.cv = threading.Condition()
-        self.queue = collections.deque()
-        self.closed = False
+        self.lock = threading.Lock()
         self.resident = collections.OrderedDict()     # geometry key -> (pts, det) on device
-        self.factors = collections.OrderedDict()      # (geometry key, k0) -> SystemFactorization
         self.factor_cache = factor_cache
         self.h2d_bytes = 0
         self.d2h_bytes = 0
@@ -137,24 +211,24 @@ class Server:
         for w in self.workers:
             w.start()
 
+    @property
+    def in_use(self):
+        """Bytes the admitted requests and cached factorisations hold."""
+        return self.admission.in_use
+
     # ---------------------------------------------------------------- API
     def submit(self, prob, pts=None, det=None):
         """Queue a request; returns a Future of its Result.  pts / det: device
         copies of the inputs when the caller already holds them."""
         fut = cf.Future()
-        need = matrix_bytes(prob, self.precision)
-        if need > self.budget:
-            fut.set_exception(MemoryError(f"request needs {need} B, above the HBM budget of {self.budget} B"))
-            return fut
-        with self.cv:
-            self.queue.append((prob, pts, det, fut, need, time.perf_counter()))
-            self.cv.notify_all()
+        try:
+            self.admission.put((prob, pts, det, fut), matrix_bytes(prob, self.precision))
+        except MemoryError as e:
+            fut.set_exception(e)
         return fut
 
     def close(self):
-        with self.cv:
-            self.closed = True
-            self.cv.notify_all()
+        self.admission.close()
         for w in self.workers:
             w.join()
 
@@ -165,39 +239,18 @@ class Server:
         self.close()
 
     # ---------------------------------------------------------------- internals
-    def _take(self):
-        with self.cv:
-            while True:
-                if self.queue:
-                    need = self.queue[0][4]
-                    # cached factorisations give way to a waiting request
-                    while self.in_use + need > self.budget and self.factors:
-                        _, old = self.factors.popitem(last=False)
-                        self.in_use -= old._held
-                    if self.in_use + need <= self.budget:
-                        self.in_use += need
-                        return self.queue.popleft()
-                elif self.closed:
-                    return None
-                self.cv.wait()
-
-    def _release(self, need):
-        with self.cv:
-            self.in_use -= need
-            self.cv.notify_all()
-
     def _geometry(self, prob, pts, det):
         if pts is not None and det is not None:
             return pts, det
         key = (prob.kind, prob.seed, prob.N)
-        with self.cv:
+        with self.lock:
             hit = self.resident.get(key)
             if hit is not None:
                 self.resident.move_to_end(key)
                 return hit
         pts = prob.points.to(self.device, non_blocking=False)
         det = prob.detectors.to(self.device, non_blocking=False)
-        with self.cv:
+        with self.lock:
             self.h2d_bytes += prob.points.numel() * 8 + prob.detectors.numel() * 8
             self.resident[key] = (pts, det)
             while len(self.resident) > 64:
@@ -208,22 +261,12 @@ class Server:
         """Cached factorisation for (geometry, k0), built on a miss.  Cached
         factorisations count against the HBM budget until evicted."""
         key = (prob.kind, prob.seed, prob.N, prob.k0)
-        with self.cv:
-            fac = self.factors.get(key)
-            if fac is not None:
-                self.factors.move_to_end(key)
-                return fac, True
+        fac = self.admission.cache_get(key)
+        if fac is not None:
+            return fac, True
         shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
         fac = E.SystemFactorization(prob.kind, pts, prob.k0, prob.alpha * prob.k0 * prob.k0, shift, self.precision)
-        held = matrix_bytes(prob, self.precision)
-        with self.cv:
-            self.factors[key] = fac
-            fac._held = held
-            self.in_use += held
-            while len(self.factors) > self.factor_cache:
-                _, old = self.factors.popitem(last=False)
-                self.in_use -= old._held
-            self.cv.notify_all()
+        self.admission.cache_put(key, fac, matrix_bytes(prob, self.precision), self.factor_cache)
         return fac, False
 
     def _run(self, slot):
@@ -231,10 +274,10 @@ class Server:
         stream = torch.cuda.Stream(self.device)
         with torch.cuda.stream(stream):
             while True:
-                item = self._take()
-                if item is None:
+                got = self.admission.take()
+                if got is None:
                     return
-                prob, pts, det, fut, need, t_submit = item
+                (prob, pts, det, fut), need = got
                 try:
                     pts, det = self._geometry(prob, pts, det)
                     fac, hit = self._factorization(prob, pts) if self.factor_cache else (None, False)
@@ -243,14 +286,14 @@ class Server:
                     if self.host_results:
                         res.Ek = res.Ek.cpu()
                         res.E_det = res.E_det.cpu()
-                        with self.cv:
+                        with self.lock:
                             self.d2h_bytes += (res.Ek.numel() + res.E_det.numel()) * 16
                     stream.synchronize()
                     res.latency = time.perf_counter() - self.start - prob.arrival
-                    self._release(need)
+                    self.admission.release(need)
                     fut.set_result(res)
                 except BaseException as e:  # noqa: BLE001 -- reported through the future
-                    self._release(need)
+                    self.admission.release(need)
                     fut.set_exception(e)
 
 
