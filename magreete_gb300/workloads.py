@@ -6,8 +6,11 @@ CPU ``torch.Generator`` so every run (CPU or GPU) sees bit-identical points:
   * uniform points in the unit disk: r = sqrt(U2), phi = 2 pi U1
     (utils.uniform_unit_disk_picking, utils.py:85-98);
   * uniform points in a cube [-1/2, 1/2]^3 (lattices.poisson, lattices.py:29-31);
-  * uniform points in the unit ball via Gaussian + exponential
-    (utils.uniform_unit_ball_picking, utils.py:100-115);
+  * points in the unit ball as the reference draws them: x / sqrt(|x|^2 + E),
+    x Gaussian, E exponential with mean 1 (utils.uniform_unit_ball_picking,
+    utils.py:100-115).  The method it cites is uniform for E of mean 2; with
+    mean 1 the points sit further out (E[r^3] = 0.63 instead of 0.5), and the
+    workload keeps the reference's distribution;
   * detectors: a ring of 360 at radius 2L (magreete.py:351-353) or a
     Fibonacci sphere (utils.fibonacci_sphere, utils.py:117-136);
   * polarisability of a small dielectric object alpha = V (n^2 - 1)
