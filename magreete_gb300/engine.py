@@ -17,9 +17,7 @@ residual ``tol`` (1e-10 by default), i.e. complex128-level accuracy.
 from __future__ import annotations
 
 import ctypes
-import math
 
-import numpy as np
 import torch
 
 from . import _lib as L

@@ -1,5 +1,4 @@
 """Serving: each result is the same alone and in the mix; HBM-budget admission."""
-import numpy as np
 import pytest
 import torch
 
