@@ -1,0 +1,77 @@
+"""Host-side math of the drop-in on CPU against the reference's golden outputs:
+incident fields (plane, beam; torch ops that run on the points' device), the
+self-interaction integrals and the diagonal shift with the reference's
+complex64 rounding, and the reference's errors for unknown types."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from magreete_gb300 import selfterm
+from magreete_gb300 import sources as S
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+KINDS = ["2d_vector", "2d_scalar", "3d_vector", "3d_scalar"]
+
+
+def load(kind):
+    z = np.load(os.path.join(GOLD, f"golden_{kind}.npz"))
+    return {k: z[k] for k in z.files}
+
+
+def rel(a, b):
+    return float(np.linalg.norm((np.asarray(a) - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def source(kind, g, which, pts):
+    k0, w = float(g["k0"]), float(g["beam_w"])
+    if kind.startswith("2d"):
+        return S.source_2d(kind, which, pts, k0, g["thetas"], w)
+    p = torch.from_numpy(g["p"]) if kind == "3d_vector" else None
+    return S.source_3d(kind, which, pts, k0, torch.from_numpy(g["u"]), p, w)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_plane_and_beam_sources_match_reference(kind):
+    g = load(kind)
+    pts = torch.from_numpy(g["points"])
+    E0 = source(kind, g, "plane", pts)
+    assert E0.dtype == torch.complex128 and tuple(E0.shape) == g["E0_scat"].shape
+    assert rel(E0.numpy(), g["E0_scat"]) <= 1e-14
+    assert rel(source(kind, g, "plane", torch.from_numpy(g["det"])).numpy(), g["E0_det"]) <= 1e-14
+    assert rel(source(kind, g, "beam", pts).numpy(), g["E0_scat_beam"]) <= 1e-14
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_self_terms_match_reference(kind):
+    g = load(kind)
+    k0, a = float(g["k0"]), float(g["radius"])
+    for t, key, tol in (("Rayleigh", "si_rayleigh", 1e-14), ("full", "si_full", 1e-12)):
+        ref = complex(g[key])
+        assert abs(complex(selfterm.SELF_TERM[kind](k0, a, t)) - ref) <= tol * abs(ref)
+    with pytest.raises(NotImplementedError):
+        selfterm.SELF_TERM[kind](k0, a, "unknown")
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_diagonal_shift_rounding(kind):
+    g = load(kind)
+    k0, a, alpha = float(g["k0"]), float(g["radius"]), complex(g["alpha"])
+    exact = selfterm.diagonal_shift(kind, k0, alpha, a, reference_rounding=False)
+    assert exact == pytest.approx(alpha * k0 * k0 * complex(g["si_rayleigh"]) / selfterm.volume(kind, a), rel=1e-14)
+    rounded = selfterm.diagonal_shift(kind, k0, alpha, a)
+    # the reference multiplies by a float32 identity: the shift is a complex64 value
+    assert rounded == complex(np.complex64(exact))
+    assert selfterm.diagonal_shift(kind, k0, alpha, a, self_interaction=False) == 0j
+
+
+def test_unknown_source_raises():
+    g = load("2d_vector")
+    pts = torch.from_numpy(g["points"])
+    with pytest.raises(NotImplementedError):
+        S.source_2d("2d_vector", "laser", pts, float(g["k0"]), g["thetas"], 1.0)
+    g3 = load("3d_vector")
+    with pytest.raises(NotImplementedError):
+        S.source_3d("3d_vector", "point", torch.from_numpy(g3["points"]), float(g3["k0"]),
+                    torch.from_numpy(g3["u"]), torch.from_numpy(g3["p"]), 1.0)
