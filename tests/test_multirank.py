@@ -73,3 +73,26 @@ def test_reference_arm_other_ranks_exit_without_work(capsys):
         steps, warmup, requests, cpu_budget, gpus = 1, 3, 2, 1.0, 2
     bench.run_reference(A, rank=1, world=2)
     assert capsys.readouterr().out == ""
+
+
+@pytest.mark.timeout(300)
+def test_reference_arm_rank0_prints_contract_line(capsys):
+    """Rank 0 of the reference arm prints one JSON line with the bench keys
+    (the oracle port's rate; a tiny calibration budget keeps this short)."""
+    import json
+    import bench
+
+    class A:
+        steps, warmup, requests, cpu_budget, gpus = 1, 3, 2, 0.01, 1
+    bench.run_reference(A, rank=0, world=1)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "solves/s"
+    for key in ("metric", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["vs_baseline"] is None and d["higher_is_better"] is True and d["config"]["workload"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
