@@ -180,6 +180,29 @@ _GREENS = {"2d_vector": greens_2d_vector, "2d_scalar": greens_2d_scalar,
            "3d_vector": greens_3d_vector, "3d_scalar": greens_3d_scalar}
 
 
+def periodic_wrap(kind, r, periodic=""):
+    """Minimum-image wrap of separations into [-1/2, 1/2) along the periodic
+    axes: (r + 1/2) mod 1 - 1/2 with a floored modulo.
+    QUIRK: the 2D classes honour exactly periodic == 'x' or 'y' (an 'xy'
+    string wraps nothing, Transmission2D.py:74-81, :605-612); the 3D classes
+    wrap every axis named in the string (Transmission3D.py:58-69, :584-595).
+    Returns a new array (the reference edits its argument in place)."""
+    r = np.array(r, dtype=np.float64, copy=True)
+    dim, _ = kind_dims(kind)
+    axes = ([{"x": 0, "y": 1}[periodic]] if periodic in ("x", "y") else []) if dim == 2 else \
+        [a for a, c in enumerate("xyz") if c in periodic]
+    for a in axes:
+        r[..., a] = np.mod(r[..., a] + 0.5, 1.0) - 0.5
+    return r
+
+
+def greens_separations(kind, r, k0, periodic="", regularize=False, radius=0.0):
+    """torch_greens / greens of the solver classes on an array of separations
+    (Transmission2D.py:63-91, :595-618; Transmission3D.py:47-77, :573-601):
+    the periodic wrap, then the kind's Green's function."""
+    return _GREENS[kind](periodic_wrap(kind, r, periodic), k0, regularize=regularize, radius=radius)
+
+
 def G0(kind, scat, k0, points=None, regularize=False, radius=0.0):
     """Dense propagator matrix, following G0_vector (Transmission2D.py:263-280),
     G0 (Transmission2D.py:777-785), G0 (Transmission3D.py:240-268, 751-777).

@@ -2,7 +2,8 @@
 
 Run from the repository root on a machine that has the reference checkout:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference            # golden_<kind>.npz
+    python tests/golden/make_golden.py /root/reference --greens   # golden_greens_<kind>.npz
 
 The reference imports ``hickle``, ``matplotlib`` and ``cmasher`` at module
 level; none of them is used on the solve path, so empty stand-in modules are
@@ -149,5 +150,47 @@ def main(ref_path):
         print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def main_greens(ref_path):
+    """golden_greens_<kind>.npz: the classes' Green's function on an array of
+    separations (torch_greens / greens), free and with each periodic option,
+    plus one regularised call in which the shortest separation falls under the
+    threshold.  Separate files, so the fixtures above stay as they are."""
+    _stub_modules()
+    sys.path.insert(0, ref_path)
+    import torch
+    import utils  # noqa: F401 -- first: utils and the solver modules import each other
+    from Transmission2D import Transmission2D_vector, Transmission2D_scalar
+    from Transmission3D import Transmission3D_vector, Transmission3D_scalar
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    classes = {"2d_vector": (Transmission2D_vector, 2, ("", "x", "y", "xy")),
+               "2d_scalar": (Transmission2D_scalar, 2, ("", "x", "y", "xy")),
+               "3d_vector": (Transmission3D_vector, 3, ("", "x", "xy", "xyz")),
+               "3d_scalar": (Transmission3D_scalar, 3, ("", "x", "xy", "xyz"))}
+    k0 = 2 * np.pi * 3.0
+    for seed, (kind, (cls, dim, options)) in enumerate(classes.items()):
+        rng = np.random.default_rng(500 + seed)
+        r = rng.uniform(-1.2, 1.2, size=(5, 4, dim))
+        r[0, 0] = 0.01                       # a short separation for the regularised call
+        # the 2D vector class compares k*R with the radius (a quirk), the others R
+        radius_reg = 0.5 if kind == "2d_vector" else 0.03
+        solver = cls(torch.from_numpy(rng.random((3, dim))), source="plane")
+        fn = solver.torch_greens if dim == 2 else solver.greens
+        res = {"r": r, "k0": k0, "radius_reg": radius_reg, "periodic_options": np.array(options)}
+        with contextlib.redirect_stdout(io.StringIO()):
+            for i, per in enumerate(options):
+                # the reference wraps its argument in place: hand it a copy
+                res[f"G_{i}"] = fn(torch.from_numpy(r.copy()), k0, periodic=per).numpy()
+            res["G_reg"] = fn(torch.from_numpy(r.copy()), k0, regularize=True, radius=radius_reg).numpy()
+        path = os.path.join(out_dir, f"golden_greens_{kind}.npz")
+        np.savez_compressed(path, **res)
+        print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MAGREETE_REFERENCE", "reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else os.environ.get("MAGREETE_REFERENCE", "reference")
+    if "--greens" in sys.argv:
+        main_greens(ref)
+    else:
+        main(ref)

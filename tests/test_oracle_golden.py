@@ -137,3 +137,23 @@ def test_known_answers():
         P = rng.random((20, dim))
         Mt = O.system_matrix(kind, P, k0, alpha, a)
         assert rel(Mt, Mt.T) < 1e-14
+
+
+@pytest.mark.parametrize("kind", O.KINDS)
+def test_greens_of_separations_periodic_and_regularised(kind):
+    """torch_greens / greens on an array of separations (free, each periodic
+    option, regularised) against the reference's outputs.  Non-finite entries
+    (a regularised separation at zero) must sit in the same places."""
+    z = np.load(os.path.join(GOLD, f"golden_greens_{kind}.npz"))
+    r, k0 = z["r"], float(z["k0"])
+    for i, per in enumerate(z["periodic_options"]):
+        G = O.greens_separations(kind, r, k0, periodic=str(per))
+        assert G.shape == z[f"G_{i}"].shape
+        assert rel(G, z[f"G_{i}"]) < tol(kind, 1e-13), per
+    G = O.greens_separations(kind, r, k0, regularize=True, radius=float(z["radius_reg"]))
+    ref = z["G_reg"]
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(G), fin) and not fin.all()
+    assert rel(G[fin], ref[fin]) < tol(kind, 1e-13)
+    # the reference's wrap changes the answer: periodic and free calls differ
+    assert not np.allclose(z["G_0"], z["G_1"])
