@@ -40,6 +40,25 @@ def _home_device(*xs):
     return torch.device("cpu")
 
 
+def periodic_wrap(r, periodic, dim):
+    """Separations r (..., dim) wrapped into [-1/2, 1/2) along the periodic
+    axes, (r + 1/2) mod 1 - 1/2 with a floored modulo, as a new float64
+    tensor (the reference edits its argument in place).  The 2D classes honour
+    exactly one of 'x' / 'y' (Transmission2D.py:74-81, :605-612: an 'xy'
+    string wraps nothing); the 3D classes wrap every axis named
+    (Transmission3D.py:58-69, :584-595)."""
+    r = _as_tensor(r).to(torch.float64).clone()
+    if periodic:
+        axes = {"x": 0, "y": 1, "z": 2}
+        if dim == 2:
+            sel = [axes[periodic]] if periodic in ("x", "y") else []
+        else:
+            sel = [axes[c] for c in "xyz" if c in periodic]
+        for a in sel:
+            r[..., a] = torch.remainder(r[..., a] + 0.5, 1.0) - 0.5
+    return r
+
+
 class CoupledDipoleSolver:
     kind = None  # "2d_vector" | "2d_scalar" | "3d_vector" | "3d_scalar"
 
@@ -83,16 +102,7 @@ class CoupledDipoleSolver:
     # ------------------------------------------------------------ Green's functions
     def _greens_of_separations(self, r, k0, periodic="", regularize=False, radius=0.0):
         """Green's tensor for an array of separations r (..., dim)."""
-        r = _as_tensor(r).to(torch.float64).clone()
-        if periodic:
-            axes = {"x": 0, "y": 1, "z": 2}
-            if self.dim == 2:
-                # the 2D classes honour exactly one of 'x' / 'y' (Transmission2D.py:74-81)
-                sel = [axes[periodic]] if periodic in ("x", "y") else []
-            else:
-                sel = [axes[c] for c in "xyz" if c in periodic]  # Transmission3D.py:58-69
-            for a in sel:
-                r[..., a] = torch.remainder(r[..., a] + 0.5, 1.0) - 0.5
+        r = periodic_wrap(r, periodic, self.dim)
         lead = r.shape[:-1]
         seps = E.points_to(r, self._dev, self.dim)
         origin = torch.zeros((1, self.dim), dtype=torch.float64, device=self._dev)
