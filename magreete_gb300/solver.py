@@ -136,6 +136,10 @@ class CoupledDipoleSolver:
         E0t = _as_tensor(E0)
         flat = E0t.dim() == 1
         B = E0t.reshape(self.d * self.N, -1).to(device=self._dev, dtype=torch.complex128).contiguous()
+        if B.shape[1] == 0:
+            # no incident fields: the reference's solve returns an empty (d*N, 0) tensor
+            self.last_stats = {}
+            return torch.zeros((self.d * self.N, 0), dtype=torch.complex128, device=home)
         stats = {}
         X = E.solve_system(self.kind, self._r_dev, k0, alpha * k0 * k0,
                            self._shift(k0, alpha, radius, self_interaction, self_interaction_type), B,

@@ -94,3 +94,23 @@ def test_periodic_wrap_matches_reference_semantics(kind):
     assert torch.equal(r, torch.from_numpy(z["r"]))
     if dim == 2:
         assert torch.equal(periodic_wrap(r, "xy", 2), r)      # the 2D classes ignore 'xy'
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_solve_without_incident_fields_returns_empty(kind, monkeypatch):
+    """solve() with zero right-hand sides returns an empty (d*N, 0) complex128
+    tensor, as the reference's linalg.solve does, without any device work (the
+    device lookup is pointed at the CPU here; no library call is reached)."""
+    import magreete_gb300 as M
+    from magreete_gb300 import engine as E
+    monkeypatch.setattr(E, "device_of", lambda *t: torch.device("cpu"))
+    cls = {"2d_vector": M.Transmission2D_vector, "2d_scalar": M.Transmission2D_scalar,
+           "3d_vector": M.Transmission3D_vector, "3d_scalar": M.Transmission3D_scalar}[kind]
+    g = load(kind)
+    s = cls(torch.from_numpy(g["points"]), source="plane")
+    d = s.d
+    E0 = torch.zeros((s.N, d, 0) if d > 1 else (s.N, 0), dtype=torch.complex128)
+    X = s.solve(float(g["k0"]), complex(g["alpha"]), float(g["radius"]), E0)
+    assert X.shape == (d * s.N, 0) and X.dtype == torch.complex128 and X.device.type == "cpu"
+    with pytest.raises(NotImplementedError):
+        s.solve(float(g["k0"]), complex(g["alpha"]), float(g["radius"]), E0, self_interaction_type="other")
