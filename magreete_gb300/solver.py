@@ -229,6 +229,10 @@ class CoupledDipoleSolver:
         Transmission3D.py:270-323, :779-832).  Returns a 0-d float64 tensor."""
         P = _as_tensor(measure_points).reshape(-1, self.dim).shape[0]
         self._say(f"Computing mean DOS using {P} points at k0L/2pi = {self._k_label(k0)}")
+        if P == 0:
+            # the reference averages over no points: 0 / 0 = nan
+            selfterm.SELF_TERM[self.kind](k0, radius, self_interaction_type)
+            return torch.tensor(float("nan"), dtype=torch.float64, device=_home_device(measure_points, self.r))
         fac = self._factorization(k0, alpha, radius, self_interaction, self_interaction_type)
         dots = self._dos_terms(fac, measure_points, k0, radius, self_interaction, self_interaction_type, regularize)
         total = dots.sum() / P
@@ -248,6 +252,9 @@ class CoupledDipoleSolver:
         """LDOS at each measurement point (Transmission2D.py:338-390, :843-890;
         Transmission3D.py:325-376, :834-886)."""
         P = _as_tensor(measure_points).reshape(-1, self.dim).shape[0]
+        if P == 0:
+            # the reference fails reshaping an empty propagator (a RuntimeError)
+            raise RuntimeError("LDOS_measurements needs at least one measurement point")
         fac = self._factorization(k0, alpha, radius, self_interaction, self_interaction_type)
         dots = self._dos_terms(fac, measure_points, k0, radius, self_interaction, self_interaction_type, regularize)
         return self._ldos_from_dots(dots, P, k0, alpha, discard_absorption).to(_home_device(measure_points, self.r))

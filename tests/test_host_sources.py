@@ -114,3 +114,25 @@ def test_solve_without_incident_fields_returns_empty(kind, monkeypatch):
     assert X.shape == (d * s.N, 0) and X.dtype == torch.complex128 and X.device.type == "cpu"
     with pytest.raises(NotImplementedError):
         s.solve(float(g["k0"]), complex(g["alpha"]), float(g["radius"]), E0, self_interaction_type="other")
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_dos_at_no_points_as_reference(kind, monkeypatch):
+    """Mean DOS over zero measurement points is nan (the reference's 0 / 0);
+    LDOS at zero points raises RuntimeError, as the reference does.  Both are
+    decided on the host before any device work."""
+    import magreete_gb300 as M
+    from magreete_gb300 import engine as E
+    monkeypatch.setattr(E, "device_of", lambda *t: torch.device("cpu"))
+    cls = {"2d_vector": M.Transmission2D_vector, "2d_scalar": M.Transmission2D_scalar,
+           "3d_vector": M.Transmission3D_vector, "3d_scalar": M.Transmission3D_scalar}[kind]
+    g = load(kind)
+    s = cls(torch.from_numpy(g["points"]), source="plane")
+    none = torch.zeros((0, s.dim), dtype=torch.float64)
+    k0, alpha, a = float(g["k0"]), complex(g["alpha"]), float(g["radius"])
+    v = s.mean_DOS_measurements(none, k0, alpha, a)
+    assert v.dim() == 0 and v.dtype == torch.float64 and torch.isnan(v)
+    with pytest.raises(NotImplementedError):
+        s.mean_DOS_measurements(none, k0, alpha, a, self_interaction_type="other")
+    with pytest.raises(RuntimeError):
+        s.LDOS_measurements(none, k0, alpha, a)
