@@ -115,6 +115,9 @@ class CoupledDipoleSolver:
         scatterers, shape (d*M, d*N) complex128 (G0_vector / G0)."""
         self._say(f"Calculating Green's function at k0L/2pi = {self._k_label(k0)} ({print_statement})")
         tg = self._r_dev if points is None else self._pts(points)
+        if tg.shape[0] == 0:
+            # no target points: an empty (0, d*N) propagator, as the reference's
+            return torch.zeros((0, self.d * self.N), dtype=torch.complex128, device=_home_device(points, self.r))
         G = E.assemble_propagator(self.kind, tg, self._r_dev, k0, 1.0, regularize, radius)
         if zero_self is None:
             zero_self = points is None

@@ -136,3 +136,19 @@ def test_dos_at_no_points_as_reference(kind, monkeypatch):
         s.mean_DOS_measurements(none, k0, alpha, a, self_interaction_type="other")
     with pytest.raises(RuntimeError):
         s.LDOS_measurements(none, k0, alpha, a)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_G0_to_no_points_is_empty(kind, monkeypatch):
+    """G0 / G0_vector towards zero target points: an empty (0, d*N) complex128
+    propagator, as the reference returns (decided on the host)."""
+    import magreete_gb300 as M
+    from magreete_gb300 import engine as E
+    monkeypatch.setattr(E, "device_of", lambda *t: torch.device("cpu"))
+    cls = {"2d_vector": M.Transmission2D_vector, "2d_scalar": M.Transmission2D_scalar,
+           "3d_vector": M.Transmission3D_vector, "3d_scalar": M.Transmission3D_scalar}[kind]
+    g = load(kind)
+    s = cls(torch.from_numpy(g["points"]), source="plane")
+    fn = s.G0_vector if kind == "2d_vector" else s.G0
+    G = fn(torch.zeros((0, s.dim), dtype=torch.float64), float(g["k0"]))
+    assert G.shape == (0, s.d * s.N) and G.dtype == torch.complex128 and G.device.type == "cpu"
