@@ -152,3 +152,20 @@ def test_G0_to_no_points_is_empty(kind, monkeypatch):
     fn = s.G0_vector if kind == "2d_vector" else s.G0
     G = fn(torch.zeros((0, s.dim), dtype=torch.float64), float(g["k0"]))
     assert G.shape == (0, s.d * s.N) and G.dtype == torch.complex128 and G.device.type == "cpu"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_sources_for_no_incidences_have_the_reference_shapes(kind):
+    """Zero angles / directions give empty fields shaped like the reference's:
+    (N, d, 0) for the vector kinds, (N, 0) for the scalar kinds."""
+    g = load(kind)
+    pts = torch.from_numpy(g["points"])
+    N, vec = pts.shape[0], kind.endswith("vector")
+    d = int(kind[0]) if vec else 1
+    for which in ("plane", "beam"):
+        if kind.startswith("2d"):
+            E0 = S.source_2d(kind, which, pts, float(g["k0"]), np.array([]), 0.2)
+        else:
+            u = torch.zeros((0, 3), dtype=torch.float64)
+            E0 = S.source_3d(kind, which, pts, float(g["k0"]), u, u if vec else None, 0.2)
+        assert tuple(E0.shape) == ((N, d, 0) if vec else (N, 0)) and E0.dtype == torch.complex128
