@@ -169,3 +169,27 @@ def test_sources_for_no_incidences_have_the_reference_shapes(kind):
             u = torch.zeros((0, 3), dtype=torch.float64)
             E0 = S.source_3d(kind, which, pts, float(g["k0"]), u, u if vec else None, 0.2)
         assert tuple(E0.shape) == ((N, d, 0) if vec else (N, 0)) and E0.dtype == torch.complex128
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_class_attributes_and_options(kind, monkeypatch):
+    """The reference's attributes (.r, .N, .source), the engine options and
+    their validation, without device work."""
+    import magreete_gb300 as M
+    from magreete_gb300 import engine as E
+    monkeypatch.setattr(E, "device_of", lambda *t: torch.device("cpu"))
+    cls = {"2d_vector": M.Transmission2D_vector, "2d_scalar": M.Transmission2D_scalar,
+           "3d_vector": M.Transmission3D_vector, "3d_scalar": M.Transmission3D_scalar}[kind]
+    g = load(kind)
+    pts = torch.from_numpy(g["points"])
+    s = cls(pts)
+    assert s.source == "beam" and s.N == pts.shape[0] and torch.equal(s.r, pts)
+    assert s.precision == "fp64"
+    assert cls(g["points"], source="plane", precision="mixed").precision == "mixed"   # numpy input too
+    monkeypatch.setenv("MAGREETE_PRECISION", "mixed")
+    assert cls(pts).precision == "mixed"
+    with pytest.raises(ValueError):
+        cls(pts, precision="fp16")
+    for name in ("compute_hamiltonian_DOS", "compute_eigenvalues_and_scatterer_LDOS", "compute_eigenmodes_IPR"):
+        with pytest.raises(NotImplementedError):
+            getattr(s, name)()
