@@ -123,3 +123,21 @@ def test_tuning_keys_round_trip_and_range_checks():
         for k, v in saved.items():
             lib.mgt_set_tuning(k, v)
     assert {k: lib.mgt_get_tuning(k) for k in keys} == saved
+
+
+def test_python_constants_match_the_header():
+    """Every #define MGT_* of the header has the same value in _lib.py, and
+    every tuning key is documented in INTEGRATION.md."""
+    from magreete_gb300 import _lib
+    defines = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        for name, val in re.findall(r"#define\s+(MGT_\w+)\s+\(?(-?\d+)\)?", open(h).read()):
+            defines[name] = int(val)
+    assert len(defines) >= 25
+    for name, val in defines.items():
+        assert hasattr(_lib, name), name
+        assert getattr(_lib, name) == val, name
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    for name in defines:
+        if name.startswith("MGT_TUNE_"):
+            assert name in doc, f"{name} missing from INTEGRATION.md"
