@@ -9,19 +9,26 @@ earlier geometry at a new frequency.  Each request is solved with the mixed
 method (complex64 LU + double-float refinement to a 1e-10 relative residual)
 and propagated to 360 (2D) / 1024 (3D) detectors.
 
-value: requests/s with inputs resident in HBM (all ranks' requests / max time).
-e2e:   the same windows through the public solver-class API with host
-       (numpy) inputs and host results, copies inside the timed region.
+value:  requests/s with inputs resident in HBM (all ranks' requests / max time).
+e2e:    the same windows through the public Server API with host inputs and
+        host results, copies inside the timed region.
+subset: the GPU's solves/s on exactly the requests the CPU arms run whole
+        (order n = dN <= 6000 of every timed window).
+vs_plain_fp64: the plain FP64 GPU method, one request at a time, against the
+        mixed server on the requests of order n <= 16000 of four timed windows,
+        with the field error of every mixed result against FP64.
+sweep:  the 256-instance batched 2D sweep in captured CUDA graphs.
 
 --impl reference times the reference algorithm's CPU implementation (the
-numpy/scipy port in oracle/, the reference itself cannot travel) on a
-bounded, size-capped sample of each window.
+numpy/scipy port in oracle/; the reference itself cannot travel) on the CPU
+subset of every timed window, each request run whole.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -53,8 +60,9 @@ def parse():
     ap.add_argument("--requests", type=int, default=8, help="requests per step (window)")
     ap.add_argument("--slots", type=int, default=4, help="requests in flight in the server")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the plain-FP64 comparison, the batched sweep and the CPU extrapolation")
     ap.add_argument("--phases", action="store_true",
                     help="print per-phase device times of the transmission configs instead of the stream bench")
     ap.add_argument("--only", default=None, help="with --phases: one case label, e.g. 3d_N4000:mixed")
@@ -64,6 +72,9 @@ def parse():
     ap.add_argument("--compare-fp64", action="store_true",
                     help="the timed windows served by the mixed server and by the plain FP64 method one request "
                          "at a time: throughput, latency and field error of the mixed results against FP64")
+    ap.add_argument("--cfg4-fp64", action="store_true",
+                    help="the large strong-scattering 3D case, mixed against the plain FP64 method (fields, DOS)")
+    ap.add_argument("--cfg4-n", type=int, default=20000, help="with --cfg4-fp64: number of points")
     return ap.parse_args()
 
 
@@ -148,9 +159,48 @@ def windows(steps, warmup, per_step, rank):
 
 # ------------------------------------------------------------------ CPU (reference algorithm)
 
+# The CPU legs run whole requests only: the requests of order n = d N <= 6000
+# of each window (about half of them; the larger ones take minutes each on
+# the host).  The GPU line reports its own solves/s on exactly these requests
+# under "subset", so the two arms can be compared like for like.
+CPU_SUBSET_N = 6000
+# The plain FP64 GPU method, one request at a time, on the requests of order
+# n <= 16000 of the first four timed windows (~30 s of complex128 LU).
+FP64_SUBSET_N = 16000
+FP64_SUBSET_WINDOWS = 4
+SUBSET_NOTE = (f"requests of order n = dN <= {CPU_SUBSET_N} of every timed window, run whole on the CPU "
+               f"(the GPU arm's 'subset' key: the same requests on the GPU)")
+
+
+def subset_indices(window, n_max):
+    return [i for i, p in enumerate(window) if p.n <= n_max]
+
+
+def host_info():
+    """Host CPU model, thread count and the BLAS numpy calls (for the CPU lines)."""
+    info = {"threads": os.cpu_count(), "machine": platform.machine()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                info["cpu_model"] = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    try:
+        cfg = np.show_config(mode="dicts")
+        blas = cfg["Build Dependencies"]["blas"]
+        info["blas"] = f"{blas.get('name')} {blas.get('version', '')}".strip()
+    except Exception:
+        pass
+    info["numpy"] = np.__version__
+    return info
+
+
 def cpu_request_time(prob):
     """Seconds the numpy/scipy port of the reference algorithm takes for one
-    request: sources, complex128 solve, propagate (all host threads)."""
+    request, run whole: sources at the scatterers and detectors, complex128
+    solve (LAPACK, all host threads), propagation to the detectors."""
     from oracle import oracle as O
     t0 = time.perf_counter()
     pts, det = prob.points.numpy(), prob.detectors.numpy()
@@ -165,16 +215,24 @@ def cpu_request_time(prob):
     return time.perf_counter() - t0
 
 
-# calibration sizes (N) per dimension: the CPU times of the stream's larger
-# requests (minutes each) are extrapolated from these
-CPU_CAL = {"2d": (500, 1000, 1800), "3d": (300, 600, 1000)}
+def cpu_measure(wins):
+    """Every CPU-subset request of `wins`, run whole: (requests, seconds, per-window seconds)."""
+    count, per = 0, []
+    t0 = time.perf_counter()
+    for w in wins:
+        ts = time.perf_counter()
+        for i in subset_indices(w, CPU_SUBSET_N):
+            cpu_request_time(w[i])
+            count += 1
+        per.append(time.perf_counter() - ts)
+    return count, time.perf_counter() - t0, per
 
 
-def cpu_calibrate(budget):
-    """Model of the port's time per request, t(n, R) = (8/3 n^3 + 8 n^2 R) / rate + b n^2:
-    `rate` is the measured complex128 LAPACK solve rate (n = 4000, 64 RHS), b (Green's
-    matrix assembly, sources, propagation) is fitted per dimension to request
-    timings at the CPU_CAL sizes."""
+def cpu_extrapolate(problems):
+    """A labelled extrapolation, not a measurement: the port's time for every
+    request of `problems` (the larger ones included), costed as
+    (8/3 n^3 + 8 n^2 R) / rate + b n^2 with the complex128 LAPACK rate measured
+    at n = 4000 and b fitted per dimension to whole requests at small N."""
     from magreete_gb300 import workloads as W
     rng = np.random.default_rng(0)
     n0, r0 = 4000, 64
@@ -186,68 +244,69 @@ def cpu_calibrate(budget):
     rate = (8 / 3 * n0 ** 3 + 8 * n0 ** 2 * r0) / (time.perf_counter() - t0)
     del A
     fits, meas = {}, []
-    t_start = time.perf_counter()
-    for dim in ("2d", "3d"):
+    for dim, sizes in (("2d", (500, 1000)), ("3d", (300, 600))):
         xs, ys = [], []
-        for N in CPU_CAL[dim]:
-            if time.perf_counter() - t_start > budget and xs:
-                break
+        for N in sizes:
             prob = (W.disk_problem(N, 17 + N, 15.0, n_angles=32) if dim == "2d"
                     else W.cube_problem(N, 17 + N, 15.0, n_dirs=16))
             t = cpu_request_time(prob)
-            lu = (8 / 3 * prob.n ** 3 + 8 * prob.n ** 2 * prob.nrhs) / rate
             xs.append(float(prob.n) ** 2)
-            ys.append(max(t - lu, 0.0))
+            ys.append(max(t - (8 / 3 * prob.n ** 3 + 8 * prob.n ** 2 * prob.nrhs) / rate, 0.0))
             meas.append((dim, N, round(t, 3)))
         fits[dim] = float(np.dot(xs, ys) / np.dot(xs, xs))
-    return {"rate": rate, "b": fits}, meas
+    t = sum((8 / 3 * p.n ** 3 + 8 * p.n ** 2 * p.nrhs) / rate + fits["2d" if p.kind.startswith("2d") else "3d"] * p.n ** 2
+            for p in problems)
+    return {"value": len(problems) / t, "unit": "solves/s", "kind": "extrapolation (not a measurement)",
+            "lapack_gflops_n4000": rate / 1e9, "calibration_requests": meas,
+            "model": "(8/3 n^3 + 8 n^2 R)/rate + b n^2 per request, b fitted per dimension"}
 
 
-def cpu_predict(problems, model):
-    t = 0.0
-    for prob in problems:
-        n, R = prob.n, prob.nrhs
-        b = model["b"]["2d" if prob.kind.startswith("2d") else "3d"]
-        t += (8 / 3 * n ** 3 + 8 * n ** 2 * R) / model["rate"] + b * n * n
-    return t
-
-
-def cpu_baseline_line(problems, budget):
-    model, meas = cpu_calibrate(budget)
-    t = cpu_predict(problems, model)
-    cores = os.cpu_count()
-    sample = (f"numpy/scipy port of the reference algorithm (complex128 solve + propagate, {cores} host threads): "
-              f"LAPACK complex128 solve rate measured at n=4000 ({model['rate'] / 1e9:.0f} GFLOP/s) and whole requests "
-              f"measured at {meas} (dim, N, seconds); each of the {len(problems)} stream requests is costed as "
-              f"(8/3 n^3 + 8 n^2 R)/rate + b n^2 with b fitted per dimension to those requests (larger requests take "
-              f"minutes each on the CPU): an extrapolation from measurements, not a measurement of every request")
-    return len(problems) / t, cores, sample
+def config_dict(args):
+    """The workload description both arms print (the same dict in both lines)."""
+    return {"workload": WORKLOAD, "requests_per_step": args.requests,
+            "l2": "inputs larger than L2 (matrices 24 n^2 bytes on the GPU)", "subset": SUBSET_NOTE}
 
 
 def run_reference(args, rank, world):
+    """The reference algorithm on the host cores (numpy/scipy port, complex128
+    LAPACK with all host threads): each step runs the CPU-subset requests of
+    one window whole; value = those requests / the wall time of the K steps.
+    Warm-up steps run the smallest subset request of each warm-up window."""
     if rank != 0:
         return
     wins = windows(args.steps, args.warmup, args.requests, 0)
-    timed = [p for w in wins[args.warmup:] for p in w]
-    t0 = time.perf_counter()
-    val, cores, sample = cpu_baseline_line(timed, args.cpu_budget)
-    wall = time.perf_counter() - t0
+    for w in wins[:args.warmup]:
+        idx = subset_indices(w, CPU_SUBSET_N)
+        if idx:
+            cpu_request_time(min((w[i] for i in idx), key=lambda p: p.n))
+    count, wall, per = cpu_measure(wins[args.warmup:])
+    val = count / wall
+    info = host_info()
+    sample = (f"numpy/scipy port of the reference algorithm (oracle/; complex128 solve + propagate, "
+              f"{info['threads']} host threads, {info.get('blas', 'numpy BLAS')}): {count} requests of order "
+              f"n <= {CPU_SUBSET_N} from the {args.steps} timed windows, each run whole and timed")
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.requests / val,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "requests_per_step": args.requests},
-            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
-                             "calibration_wall_s": wall},
+            "data": "synthetic", "config": config_dict(args),
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": info["threads"], "kind": "port",
+                             "sample": sample, "requests": count, "seconds": wall, "host": info,
+                             "seconds_per_step": per},
             "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ GPU
 
-def e2e_window(problems, precision):
-    """Public-API pass: host numpy inputs -> solver classes -> host results."""
+def e2e_class_api(problems, precision):
+    """The requests one at a time through the drop-in solver classes with numpy
+    inputs and CPU results (the reference's plugin boundary): generate_source
+    -> solve -> propagate, as the reference driver runs them per frequency.
+    Returns (seconds, host-to-device bytes, device-to-host bytes)."""
     from magreete_gb300 import Transmission2D_vector, Transmission3D_vector
     h2d = d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     for prob in problems:
         pts, det = prob.points.numpy(), prob.detectors.numpy()
         if prob.kind.startswith("2d"):
@@ -261,9 +320,107 @@ def e2e_window(problems, precision):
             E0d = s.generate_source(det, prob.k0, u, p, 0.2)
         Ek = s.solve(prob.k0, prob.alpha, prob.radius, E0s)
         Ed = s.propagate(det, Ek, prob.k0, prob.alpha, E0d)
-        h2d += 2 * pts.nbytes + 2 * det.nbytes + E0s.numel() * 16 + Ek.numel() * 16 + E0d.numel() * 16
+        # points copied in three times (class, two sources), the detectors twice;
+        # sources, fields and detector fields each cross once per direction
+        h2d += 3 * pts.nbytes + 2 * det.nbytes + E0s.numel() * 16 + Ek.numel() * 16 + E0d.numel() * 16
         d2h += E0s.numel() * 16 + E0d.numel() * 16 + Ek.numel() * 16 + Ed.numel() * 16
-    return h2d, d2h
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, h2d, d2h
+
+
+def serve_windows(srv, wins, dev_inputs=None):
+    """Serve each window's requests at their arrival times; (results, seconds)."""
+    from magreete_gb300 import serve
+    res = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k, w in enumerate(wins):
+        res += serve.serve_stream(w, device_inputs=dev_inputs[k] if dev_inputs is not None else None, server=srv)
+    torch.cuda.synchronize()
+    return res, time.perf_counter() - t0
+
+
+def pick(wins, dev_inputs, n_max):
+    """The requests of order n <= n_max of each window (and their device inputs)."""
+    sw, sd = [], []
+    for w, di in zip(wins, dev_inputs):
+        idx = subset_indices(w, n_max)
+        sw.append([w[i] for i in idx])
+        sd.append([di[i] for i in idx])
+    return sw, sd
+
+
+def lat_stats(res):
+    lat = sorted(1e3 * r.latency for r in res)
+    return {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}
+
+
+def rel_err(a, b):
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
+def vs_plain_fp64(srv, wins, dev_inputs):
+    """The mixed server against the plain FP64 method run one request at a
+    time, on the FP64 subset: solves/s, latency, and the field error of every
+    mixed result against the FP64 one."""
+    from magreete_gb300 import serve
+    sw, sd = pick(wins, dev_inputs, FP64_SUBSET_N)
+    mixed, t_mixed = serve_windows(srv, sw, sd)
+    plain = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for w, di in zip(sw, sd):
+        plain += serve.serve_sequential(w, "fp64", di)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    n = sum(len(w) for w in sw)
+    ek = [rel_err(m.Ek, p.Ek) for m, p in zip(mixed, plain)]
+    ed = [rel_err(m.E_det, p.E_det) for m, p in zip(mixed, plain)]
+    return {"sample": f"requests of order n <= {FP64_SUBSET_N} of the first {len(sw)} timed windows",
+            "requests": n, "sizes": [(p.kind[:2], p.n, p.nrhs) for w in sw for p in w],
+            "mixed_served": {"solves_per_s": n / t_mixed, "seconds": t_mixed, "latency_ms": lat_stats(mixed),
+                             "max_rel_residual": max(r.rel_residual for r in mixed)},
+            "plain_fp64_one_at_a_time": {"solves_per_s": n / t_plain, "seconds": t_plain,
+                                         "latency_ms": lat_stats(plain)},
+            "ratio": t_plain / t_mixed,
+            "max_field_err_vs_fp64": {"Ek": max(ek), "E_det": max(ed)}}
+
+
+def sweep_measure(count, group):
+    """The batched 2D sweep (TE disk, N uniform in [500, 4000], 16 angles):
+    groups of instances captured into one CUDA graph each, concurrency and
+    panel height chosen by the autotuner on the first group; instances/s over
+    graph replays (one warm replay per group first)."""
+    from magreete_gb300 import _lib, batch
+    from magreete_gb300 import workloads as W
+    lib = _lib.load()
+    old_rows = lib.mgt_get_tuning(_lib.MGT_TUNE_PANEL_ROWS)
+    probs = W.sweep_2d(count)
+    groups = [probs[i:i + group] for i in range(0, len(probs), group)]
+    try:
+        best = batch.autotune(groups[0])
+        t_total, worst, extra_total, flops = 0.0, 0.0, 0, 0.0
+        for g in groups:
+            sw = batch.BatchedSweep(g, branches=best["branches"])
+            sw.warmup()
+            sw.capture()
+            sw.replay()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            extra, res = sw.replay()
+            t_total += time.perf_counter() - t0
+            worst = max(worst, max(res))
+            extra_total += sum(extra)
+            flops += sum(8 / 3 * p.n ** 3 for p in g)
+            del sw
+            torch.cuda.empty_cache()
+    finally:
+        lib.mgt_set_tuning(_lib.MGT_TUNE_PANEL_ROWS, old_rows)
+    return {"case": "batched 2D sweep", "instances": len(probs), "group": group,
+            "autotune": {k: v for k, v in best.items() if k != "candidates"}, "candidates": best.get("candidates"),
+            "seconds": t_total, "instances_per_s": len(probs) / t_total,
+            "lu_tflops_effective": flops / t_total / 1e12, "max_rel_residual": worst,
+            "corrections_after_graph": extra_total}
 
 
 def secondary_rooflines():
@@ -379,9 +536,20 @@ def run_ours(args, rank, world, local):
     elapsed = max_over_ranks(elapsed, world, dev)
     n_req = args.steps * args.requests * world
     value = n_req / elapsed
-    # ---- e2e through the public API with host buffers
+    # ---- the CPU subset on the GPU (the requests the CPU arms run whole), served the same way
+    sub_w, sub_d = pick(wins[args.warmup:], dev_inputs[args.warmup:], CPU_SUBSET_N)
+    sub_res, sub_t = serve_windows(srv, sub_w, sub_d)
+    n_sub = sum(len(w) for w in sub_w)
+    subset = {"value": n_sub / sub_t, "unit": "solves/s", "requests": n_sub, "seconds": sub_t,
+              "sample": SUBSET_NOTE, "latency_ms": lat_stats(sub_res)}
+    # ---- the plain FP64 method on a subset of the timed windows
+    fp64_cmp = None
+    if not args.no_extras:
+        fp64_cmp = vs_plain_fp64(srv, wins[args.warmup:args.warmup + FP64_SUBSET_WINDOWS],
+                                 dev_inputs[args.warmup:args.warmup + FP64_SUBSET_WINDOWS])
     srv.close()
-    e2e = None
+    # ---- e2e through the public API with host buffers
+    e2e = e2e_api = None
     if not args.no_e2e:
         # the same windows through the public Server API with host inputs and host
         # results: points / detectors copied in, fields copied out, inside the timed region
@@ -397,7 +565,13 @@ def run_ours(args, rank, world, local):
         esrv.close()
         e_el = max_over_ranks(e_el, world, dev)
         e2e = {"value": n_req / e_el, "unit": "solves/s", "h2d_bytes_per_step": h2d // args.steps,
-               "d2h_bytes_per_step": d2h // args.steps}
+               "d2h_bytes_per_step": d2h // args.steps, "api": "magreete_gb300.serve.Server(host_results=True)"}
+        # the first timed window through the drop-in classes, one request at a time
+        t_api, h2d_api, d2h_api = e2e_class_api(wins[args.warmup], args.precision)
+        e2e_api = {"value": len(wins[args.warmup]) / t_api, "unit": "solves/s", "requests": len(wins[args.warmup]),
+                   "h2d_bytes": h2d_api, "d2h_bytes": d2h_api,
+                   "api": "Transmission2D_vector / Transmission3D_vector: generate_source x2, solve, propagate; "
+                          "numpy in, CPU tensors out; one request at a time (first timed window)"}
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -425,23 +599,35 @@ def run_ours(args, rank, world, local):
                                f"bf16_tflops of {src} peaks",
                 "measured": "CUDA events around each launch on its stream, sequential pass over the first timed window",
                 "in_mix_tflops": (mix_flops / (mix_ms * 1e-3) / 1e12) if mix_ms > 0 else None}
-    secondary = secondary_rooflines() if rank == 0 else None
-    cpu = None
+    secondary = secondary_rooflines()
+    sweep = None if args.no_extras else sweep_measure(256, 32)
+    cpu = cpu_extra = None
     if world == 1:
-        timed = [p for w in wins[args.warmup:] for p in w]
-        val, cores, sample = cpu_baseline_line(timed, args.cpu_budget)
-        cpu = {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample}
+        first = wins[args.warmup:args.warmup + 2]
+        count, wall, _ = cpu_measure(first)
+        info = host_info()
+        cpu = {"value": count / wall, "unit": "solves/s", "cores": info["threads"], "kind": "port",
+               "sample": f"numpy/scipy port of the reference algorithm (oracle/; complex128, {info['threads']} host "
+                         f"threads, {info.get('blas', 'numpy BLAS')}): the {count} requests of order "
+                         f"n <= {CPU_SUBSET_N} of the first {len(first)} timed windows, each run whole and timed",
+               "requests": count, "seconds": wall, "host": info}
+        if not args.no_extras:
+            cpu_extra = cpu_extrapolate([p for w in wins[args.warmup:] for p in w])
     lat_ms = sorted(1e3 * x for x in lat)
+    refinement = {"max_iterations": max(iters), "max_rel_residual": max(rres)}
+    if fp64_cmp is not None:
+        refinement["max_field_err_vs_fp64"] = dict(fp64_cmp["max_field_err_vs_fp64"],
+                                                   sample=fp64_cmp["sample"])
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "complex64 LU + double-float residual" if args.precision == "mixed" else "complex128",
-            "data": "synthetic",
-            "config": {"workload": WORKLOAD, "requests_per_step": args.requests, "precision": args.precision,
-                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (matrices 24 n^2 bytes)"},
+            "data": "synthetic", "precision": args.precision, "parallelism": f"replicas x{world}",
+            "config": config_dict(args),
             "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
-            "refinement": {"max_iterations": max(iters), "max_rel_residual": max(rres)},
-            "e2e": e2e, "roofline": roofline, "roofline_other": secondary, "cpu_baseline": cpu, "clocks": clk,
+            "refinement": refinement, "subset": subset, "vs_plain_fp64": fp64_cmp, "sweep": sweep,
+            "e2e": e2e, "e2e_class_api": e2e_api, "roofline": roofline, "roofline_other": secondary,
+            "cpu_baseline": cpu, "cpu_full_stream_extrapolated": cpu_extra, "clocks": clk,
             "gpu_launches": launches}
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -550,36 +736,10 @@ def run_dos(precision=None):
 
 
 def run_sweep(args):
-    """Batched 2D sweep (TE disk, N uniform in [500, 4000], 16 angles): groups of
-    instances captured into one CUDA graph each, concurrency and panel height
-    chosen by the autotuner on the first group; instances/s over graph replays."""
-    from magreete_gb300 import _lib, batch
-    from magreete_gb300 import workloads as W
+    """The batched 2D sweep alone (see sweep_measure)."""
+    from magreete_gb300 import _lib
     _lib.load()
-    probs = W.sweep_2d(args.sweep)
-    groups = [probs[i:i + args.group] for i in range(0, len(probs), args.group)]
-    best = batch.autotune(groups[0])
-    t_total, worst, extra_total, flops = 0.0, 0.0, 0, 0.0
-    for g in groups:
-        sw = batch.BatchedSweep(g, branches=best["branches"])
-        sw.warmup()
-        sw.capture()
-        sw.replay()                              # first replay: warm
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        extra, res = sw.replay()
-        t_total += time.perf_counter() - t0
-        worst = max(worst, max(res))
-        extra_total += sum(extra)
-        flops += sum(8 / 3 * p.n ** 3 for p in g)
-        del sw
-        torch.cuda.empty_cache()
-    print(json.dumps({"case": "batched_2d_sweep", "instances": len(probs), "group": args.group,
-                      "autotune": {k: v for k, v in best.items() if k != "candidates"},
-                      "candidates": best.get("candidates"),
-                      "seconds": t_total, "instances_per_s": len(probs) / t_total,
-                      "lu_tflops_effective": flops / t_total / 1e12, "max_rel_residual": worst,
-                      "corrections_after_graph": extra_total}), flush=True)
+    print(json.dumps(sweep_measure(args.sweep, args.group)), flush=True)
 
 
 def run_compare_fp64(args):
@@ -633,11 +793,59 @@ def run_compare_fp64(args):
         "field_error_vs_fp64": {"max_rel_Ek": max(ek), "max_rel_E_det": max(ed)}}), flush=True)
 
 
+def run_cfg4_fp64(args):
+    """The large strong-scattering 3D case (unit ball, N = 20000, n = 60000,
+    n_ref = 2.0, k0 L = 2 pi 15, 128 right-hand sides, 1024 detectors) with
+    the mixed method and with the plain FP64 method (the FP64 answer at this
+    size, which the host oracle cannot hold): the error of every field and of
+    the mean DOS at 32 points in the ball of radius L/2, mixed against FP64,
+    and the time of each."""
+    from magreete_gb300 import Transmission3D_vector, _lib
+    from magreete_gb300 import workloads as W
+    _lib.load()
+    prob = W.ball_problem(args.cfg4_n, 4, 15.0)
+    mp = 0.5 * W.ball_points(32, 44)
+    dev = torch.device("cuda")
+    pts, det = prob.points.to(dev), prob.detectors.to(dev)
+    out = {"case": f"3D ball N={prob.N} (n={prob.n}), n_ref 2.0, k0L 2pi*15, {prob.nrhs} RHS, "
+                   f"{det.shape[0]} detectors; mean DOS at {len(mp)} points"}
+    res = {}
+    for prec in ("mixed", "fp64"):
+        s = Transmission3D_vector(pts, source="plane", precision=prec)
+        E0s = s.generate_source(pts, prob.k0, prob.u, prob.p, 0.2)
+        E0d = s.generate_source(det, prob.k0, prob.u, prob.p, 0.2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Ek = s.solve(prob.k0, prob.alpha, prob.radius, E0s)
+        Ed = s.propagate(det, Ek, prob.k0, prob.alpha, E0d)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        dos = float(s.mean_DOS_measurements(mp.to(dev), prob.k0, prob.alpha, prob.radius))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        res[prec] = (Ek.cpu(), Ed.cpu(), dos)
+        out[prec] = {"solve_propagate_s": t1 - t0, "mean_dos_s": t2 - t1, "stats": dict(s.last_stats),
+                     "mean_dos": dos}
+        del Ek, Ed, s
+        torch.cuda.empty_cache()
+    (Em, Dm, dm), (Ef, Df, df) = res["mixed"], res["fp64"]
+    col = lambda a, b: (torch.linalg.norm(a - b, dim=0) / torch.linalg.norm(b, dim=0)).max().item()
+    out["error_mixed_vs_fp64"] = {
+        "Ek_rel_frobenius": rel_err(Em, Ef), "Ek_worst_field": col(Em, Ef),
+        "E_det_rel_frobenius": rel_err(Dm, Df), "E_det_worst_field": col(Dm.reshape(-1, prob.nrhs),
+                                                                          Df.reshape(-1, prob.nrhs)),
+        "mean_dos_rel": abs(dm - df) / abs(df)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.compare_fp64:
         run_compare_fp64(args)
+        return
+    if args.cfg4_fp64:
+        run_cfg4_fp64(args)
         return
     if args.phases:
         run_phases(args)

@@ -24,6 +24,9 @@ Layout conventions (same as the reference):
 """
 from __future__ import annotations
 
+import concurrent.futures as _cf
+import os
+
 import numpy as np
 import scipy.special as sps
 
@@ -203,6 +206,33 @@ def greens_separations(kind, r, k0, periodic="", regularize=False, radius=0.0):
     return _GREENS[kind](periodic_wrap(kind, r, periodic), k0, regularize=regularize, radius=radius)
 
 
+# Row blocks of the dense Green's tensor are evaluated on all host threads
+# (numpy releases the GIL inside its elementwise loops), as the reference's
+# torch operations use every intra-op thread.  Each entry is computed by the
+# same elementwise expression either way, so the result does not depend on
+# the split.
+THREADS = os.cpu_count() or 1
+
+
+def _greens_rows(kind, P, scat, k0, regularize, radius):
+    M = P.shape[0]
+    f = _GREENS[kind]
+    if THREADS <= 1 or M * scat.shape[0] < 1 << 18:
+        return f(P[:, None, :] - scat[None, :, :], k0, regularize=regularize, radius=radius)
+    step = -(-M // (4 * THREADS))
+    blocks = [(a, min(M, a + step)) for a in range(0, M, step)]
+    first = f(P[:1, None, :] - scat[None, :, :], k0, regularize=regularize, radius=radius)
+    out = np.empty((M,) + first.shape[1:], first.dtype)
+
+    def one(ab):
+        a, b = ab
+        out[a:b] = f(P[a:b, None, :] - scat[None, :, :], k0, regularize=regularize, radius=radius)
+
+    with _cf.ThreadPoolExecutor(THREADS) as ex:
+        list(ex.map(one, blocks))
+    return out
+
+
 def G0(kind, scat, k0, points=None, regularize=False, radius=0.0):
     """Dense propagator matrix, following G0_vector (Transmission2D.py:263-280),
     G0 (Transmission2D.py:777-785), G0 (Transmission3D.py:240-268, 751-777).
@@ -217,8 +247,7 @@ def G0(kind, scat, k0, points=None, regularize=False, radius=0.0):
     dim, d = kind_dims(kind)
     self_pairs = points is None
     P = scat if self_pairs else points
-    sep = P[:, None, :] - scat[None, :, :]
-    g = _GREENS[kind](sep, k0, regularize=regularize, radius=radius)
+    g = _greens_rows(kind, P, scat, k0, regularize, radius)
     M, N = P.shape[0], scat.shape[0]
     if self_pairs and kind != "2d_scalar":
         idx = np.arange(N)
