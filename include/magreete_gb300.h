@@ -114,9 +114,15 @@ int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm,
  * until the process exits; n is limited to 65536 (larger: MGT_ERR_UNSUPPORTED).
  * All calls share that array: calls whose GPU work overlaps race on it, so
  * serialise them.  The first call on a device looks up the array's device
- * address; make it before any stream capture.  info (device, 2 x int32, may
- * be NULL) receives the status words: [0] device error, [1] first zero pivot
- * (1-based, 0 if none).  Allocates no device memory.
+ * address (and sets the kernels' shared-memory limits on that device); make
+ * it before any stream capture.  The address is kept for the life of the
+ * process, so the library does not survive a cudaDeviceReset.  info (device,
+ * 2 x int32, may be NULL) receives the status words: [0] device error, [1]
+ * first zero pivot (1-based, 0 if none).  They are copied into info on
+ * `stream`, in stream order, from the shared array: read them only after
+ * synchronising the stream, and only under the same rule as the scratch (a
+ * later call whose work overlaps can overwrite the words before the copy).
+ * Allocates no device memory.
  */
 int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, int32_t* info,
                          void* stream);
@@ -139,9 +145,10 @@ int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_
  * trailing update A22 -= L21 U12 (inside ?getrf of torch.linalg.solve,
  * Transmission2D.py:230 / Transmission3D.py:205), exposed on its own.
  * MGT_C128: FP64 SIMT.  MGT_C64 with use_tensor_cores = 0: FP32 SIMT;
- * use_tensor_cores = 1: tcgen05 kind::tf32 with hi/lo split operands
- * (TF32x3, FP32-level accuracy), K <= 128, ldc even; needs
- * mgt_cgemm_workspace_bytes(max(M, N)) bytes of workspace.
+ * use_tensor_cores = 1: tcgen05 tensor cores with hi/lo split operands
+ * (FP32-level accuracy; the scheme is MGT_TUNE_TC_PRECISION: F16x2 with
+ * kind::f16 by default, or TF32x3 with kind::tf32), K <= 128, ldc even;
+ * needs mgt_cgemm_workspace_bytes(max(M, N)) bytes of workspace.
  */
 int mgt_cgemm_workspace_bytes(int64_t nmax, size_t* bytes);
 int mgt_cgemm_sub(int dtype, int use_tensor_cores, int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,

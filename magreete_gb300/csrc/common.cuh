@@ -8,9 +8,42 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <utility>
+
 #include "../../include/magreete_gb300.h"
 
 namespace mgt {
+
+// Kernel attributes (the dynamic shared-memory limit, cluster permissions)
+// belong to one device's context, and device properties can differ between
+// GPUs: set-up that records them runs once per device, the first time it is
+// needed with that device current.
+constexpr int kMaxDevices = 64;
+
+inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) d = 0;
+  return d;
+}
+
+struct OncePerDevice {
+  std::once_flag flags[kMaxDevices];
+  template <class F> void operator()(F&& f) { std::call_once(flags[current_device()], std::forward<F>(f)); }
+};
+
+// SM count of the current device (cached per device).
+inline int device_sm_count() {
+  static OncePerDevice once;
+  static int sms[kMaxDevices] = {};
+  const int d = current_device();
+  once([d] {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || v <= 0) v = 1;
+    sms[d] = v;
+  });
+  return sms[d];
+}
 
 template <typename T> struct CplxOf;
 template <> struct CplxOf<double> { using type = double2; };

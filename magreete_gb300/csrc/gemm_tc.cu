@@ -1,5 +1,7 @@
-// Tensor-core (tcgen05, kind::tf32) complex trailing update for the
-// complex64 LU:  C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 128.
+// Tensor-core (tcgen05) complex trailing update for the complex64 LU:
+//   C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 128.
+// Two split-product schemes: F16x2 with kind::f16 MMAs (the default) and
+// TF32x3 with kind::tf32 MMAs (MGT_TUNE_TC_PRECISION).
 //
 // Complex -> real: with A stored interleaved (re, im) the row of A is a real
 // row of length 2K, and
@@ -8,9 +10,9 @@
 // so C' (M x 2N real, interleaved) -= A' (M x 2K) * B' (2K x 2N), where the
 // prep kernel writes B'^T (2N rows, 2K contiguous) -- a K-major operand.
 //
-// Precision: FP32 inputs are split x = hi + lo with hi = tf32(x) (round to
+// TF32x3: FP32 inputs are split x = hi + lo with hi = tf32(x) (round to
 // nearest, low 13 bits zero) and lo = x - hi; the product is accumulated in
-// FP32 in TMEM as hi*hi + hi*lo + lo*hi ("TF32x3", the split-product scheme of
+// FP32 in TMEM as hi*hi + hi*lo + lo*hi (the split-product scheme of
 // Markidis et al. 2018 / Ootomo & Yokota 2022), which keeps ~FP32 accuracy.
 //
 // F16x2 variant (default): both operands are first scaled by a power of two
@@ -607,21 +609,11 @@ int tc_make_cmap(CUtensorMap* map, float2* C, int64_t rows, int64_t cols, int64_
              : MGT_ERR_CUDA;
 }
 
-static int tc_num_sms() {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  });
-  return sms;
-}
+static int tc_num_sms() { return device_sm_count(); }
 
 static void tc_init_attrs() {
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static OncePerDevice once;
+  once([] {
     cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)tc::smem_bytes<2, 4>());
     cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -1180,17 +1180,7 @@ __global__ void lu_start_kernel(int32_t* perm, int n, unsigned long long* epoch,
     *reinterpret_cast<unsigned long long*>(records + (size_t)r * kRecBytes) = 0ull;
 }
 
-static int num_sms() {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  });
-  return sms;
-}
+static int num_sms() { return device_sm_count(); }
 
 // Trailing update: tensor cores (tcgen05 TF32x3) for complex64 when a plan is
 // given, SIMT otherwise (complex128, or no tensor-core scratch).
@@ -1213,9 +1203,11 @@ static std::atomic<int> g_panel_cluster{1};     // complex64 panels of <= 16 CTA
 
 // Largest cluster of register panel CTAs the device schedules (16, 8 or 0).
 static int cluster_panel_max() {
-  static int cmax = -1;
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static int cmax_dev[kMaxDevices];
+  static OncePerDevice once;
+  const int dev = current_device();
+  once([dev] {
+    int& cmax = cmax_dev[dev];
     const size_t smem = reg_panel_smem(64, sizeof(float2));
     cmax = 0;
     if (cudaFuncSetAttribute(lu_panel_cluster_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -1242,7 +1234,7 @@ static int cluster_panel_max() {
     }
     cudaGetLastError();
   });
-  return cmax;
+  return cmax_dev[dev];
 }
 
 int set_sym_assembly(int v);
@@ -1272,8 +1264,8 @@ template <typename T, int NB>
 static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s,
                           const TcLU* tc = nullptr) {
   using V = cplx<T>;
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static OncePerDevice once;
+  once([] {
     cudaFuncSetAttribute(lu_panel_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemBudget);
     cudaFuncSetAttribute(lu_swap_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
@@ -1398,9 +1390,9 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   }
   // tensor-core path: 128-wide outer blocks made of two 64-wide inner panels,
   // so that the trailing update runs with K = 128 (half the C traffic per flop)
-  static std::once_flag once2;
+  static OncePerDevice once2;
   const size_t sm3 = (NB * kSwapCols + NB * (NB + 1) + NB * kSwapCols) * sizeof(V);
-  std::call_once(once2, [sm3] {
+  once2([sm3] {
     cudaFuncSetAttribute(lu_preupdate_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     if constexpr (sizeof(T) == 4)
       cudaFuncSetAttribute(lu_block_right_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1611,9 +1603,9 @@ static int lu_solve_impl(const cplx<T>* LU, int n, int64_t lda, const int32_t* p
     return e;
   }
   constexpr int BS = 64;
-  static std::once_flag once;
+  static OncePerDevice once;
   const size_t smem = (BS * BS + BS * kTrsmCols) * sizeof(V);
-  std::call_once(once, [smem] {
+  once([smem] {
     cudaFuncSetAttribute(trsm_block_kernel<T, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(trsm_block_kernel<T, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });

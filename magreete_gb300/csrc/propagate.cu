@@ -152,17 +152,7 @@ __global__ void propagate_reduce_kernel(const double2* __restrict__ partial, int
   out[r * ld_out + c] = o;
 }
 
-static int sm_count() {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  });
-  return sms;
-}
+static int sm_count() { return device_sm_count(); }
 
 static int choose_splits(int64_t nt, int64_t ns) {
   int64_t tiles = (nt + kPT - 1) / kPT;

@@ -156,16 +156,19 @@ static void launch_residual(const float4* M, int64_t ldm, const float4* Xs, int6
 // resident CTAs per SM of residual_df_kernel<RT> (1 when no device answers)
 template <int RT>
 static int residual_occupancy() {
-  static int occ = 1;
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static int occ[kMaxDevices];
+  static OncePerDevice once;
+  const int dev = current_device();
+  once([dev] {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, residual_df_kernel<RT>, 256, 0) == cudaSuccess && b > 0)
-      occ = b;
-    else
+      occ[dev] = b;
+    else {
+      occ[dev] = 1;
       cudaGetLastError();
+    }
   });
-  return occ;
+  return occ[dev];
 }
 
 // R = B - sum of the split-K partials (FP64)
@@ -184,17 +187,7 @@ __global__ void residual_reduce_kernel(const double2* __restrict__ partial, int 
   R[(int64_t)r * ldr + col_base + c] = acc;
 }
 
-static int res_num_sms() {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  });
-  return sms;
-}
+static int res_num_sms() { return device_sm_count(); }
 
 // K splits of a rows x kdim residual over ncols (<= kResCols) columns.
 // Many short CTAs balance the SMs better than a few long ones: the split

@@ -279,8 +279,8 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   const size_t smem = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
   const size_t smem_w = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
   static int max_ctas = 0, max_ctas_w = 0;
-  static std::once_flag once;
-  std::call_once(once, [smem, smem_w, smem_inv] {
+  static OncePerDevice once;
+  once([smem, smem_w, smem_inv] {
     cudaFuncSetAttribute(diag_inverse_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
     cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     max_ctas = resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTG>, smem);
@@ -327,8 +327,8 @@ template <typename T>
 int lower_block_inverses(const cplx<T>* F, int64_t ldf, int n, cplx<T>* Inv, cudaStream_t s) {
   using V = cplx<T>;
   const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kInvLd) * sizeof(V);
-  static std::once_flag once;
-  std::call_once(once, [smem_inv] {
+  static OncePerDevice once;
+  once([smem_inv] {
     cudaFuncSetAttribute(diag_inverse_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   });
   count_launch();
