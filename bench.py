@@ -13,7 +13,7 @@ value:  requests/s with inputs resident in HBM (all ranks' requests / max time).
 e2e:    the same windows through the public Server API with host inputs and
         host results, copies inside the timed region.
 subset: the GPU's solves/s on exactly the requests the CPU arms run whole
-        (order n = dN <= 6000 of every timed window).
+        (order n = dN <= 12000 of every timed window).
 vs_plain_fp64: the plain FP64 GPU method, one request at a time, against the
         mixed server on the requests of order n <= 16000 of four timed windows,
         with the field error of every mixed result against FP64.
@@ -159,11 +159,11 @@ def windows(steps, warmup, per_step, rank):
 
 # ------------------------------------------------------------------ CPU (reference algorithm)
 
-# The CPU legs run whole requests only: the requests of order n = d N <= 6000
-# of each window (about half of them; the larger ones take minutes each on
-# the host).  The GPU line reports its own solves/s on exactly these requests
+# The CPU legs run whole requests only: the requests of order n = d N <= 12000
+# of each window (about two thirds of them, ~3.5 minutes on 16 host cores for
+# 20 windows; the larger ones take up to ten minutes each on the host).  The GPU line reports its own solves/s on exactly these requests
 # under "subset", so the two arms can be compared like for like.
-CPU_SUBSET_N = 6000
+CPU_SUBSET_N = 12000
 # The plain FP64 GPU method, one request at a time, on the requests of order
 # n <= 16000 of the first four timed windows (~30 s of complex128 LU).
 FP64_SUBSET_N = 16000
