@@ -388,101 +388,37 @@ def vs_plain_fp64(srv, wins, dev_inputs):
 
 def sweep_measure(count, group):
     """The batched 2D sweep (TE disk, N uniform in [500, 4000], 16 angles):
-    groups of instances captured into one CUDA graph each, concurrency and
-    panel height chosen by the autotuner on the first group; instances/s over
-    graph replays (one warm replay per group first)."""
-    from magreete_gb300 import _lib, batch
+    groups of instances captured into one CUDA graph each, concurrency,
+    pivoting and LU block width chosen by the autotuner on the first group;
+    instances/s over graph replays (one warm replay per group first)."""
+    from magreete_gb300 import batch
     from magreete_gb300 import workloads as W
-    lib = _lib.load()
-    old_rows = lib.mgt_get_tuning(_lib.MGT_TUNE_PANEL_ROWS)
     probs = W.sweep_2d(count)
     groups = [probs[i:i + group] for i in range(0, len(probs), group)]
-    try:
-        best = batch.autotune(groups[0])
-        t_total, worst, extra_total, flops = 0.0, 0.0, 0, 0.0
-        for g in groups:
-            sw = batch.BatchedSweep(g, branches=best["branches"])
-            sw.warmup()
-            sw.capture()
-            sw.replay()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            extra, res = sw.replay()
-            t_total += time.perf_counter() - t0
-            worst = max(worst, max(res))
-            extra_total += sum(extra)
-            flops += sum(8 / 3 * p.n ** 3 for p in g)
-            del sw
-            torch.cuda.empty_cache()
-    finally:
-        lib.mgt_set_tuning(_lib.MGT_TUNE_PANEL_ROWS, old_rows)
+    best = batch.autotune(groups[0])
+    choice = {k: best[k] for k in ("branches", "pivoting", "outer_block")}
+    t_total, worst, extra_total, flops, refactored = 0.0, 0.0, 0, 0.0, 0
+    for g in groups:
+        sw = batch.BatchedSweep(g, **choice)
+        sw.warmup()
+        sw.capture()
+        sw.replay()
+        torch.cuda.synchronize()
+        sw.refactored = 0
+        t0 = time.perf_counter()
+        extra, res = sw.replay()
+        t_total += time.perf_counter() - t0
+        worst = max(worst, max(res))
+        extra_total += sum(extra)
+        refactored += sw.refactored
+        flops += sum(8 / 3 * p.n ** 3 for p in g)
+        del sw
+        torch.cuda.empty_cache()
     return {"case": "batched 2D sweep", "instances": len(probs), "group": group,
             "autotune": {k: v for k, v in best.items() if k != "candidates"}, "candidates": best.get("candidates"),
             "seconds": t_total, "instances_per_s": len(probs) / t_total,
             "lu_tflops_effective": flops / t_total / 1e12, "max_rel_residual": worst,
-            "corrections_after_graph": extra_total}
-
-
-def secondary_rooflines():
-    """The other two kernels with large shares of the stream, timed alone with
-    CUDA events after the timed region: the double-float residual (FP32 pipe;
-    3D N=4000, n = 12000, 64 right-hand sides) and the LU panel (latency: one
-    cross-CTA exchange per column; the complex64 LU of 2D N=1000, n = 2000,
-    where the trailing update is negligible)."""
-    from magreete_gb300 import engine as E, selfterm
-    from magreete_gb300 import workloads as W
-    dev = torch.device("cuda")
-    out = {}
-    prob = W.cfg2()
-    pts = prob.points.to(dev)
-    coef = prob.alpha * prob.k0 ** 2
-    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
-    (Mdf,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf",))
-    n, R = prob.n, prob.nrhs
-    X = torch.randn(n, R, dtype=torch.complex128, device=dev)
-    B = torch.randn(n, R, dtype=torch.complex128, device=dev)
-    E.residual(Mdf, X, B)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(3):
-        E.residual(Mdf, X, B)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / 3
-    macs = float(n) * n * R
-    ops = 52.0 * macs          # FP32 operations of one double-float complex multiply-add
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    clk = 2.07e9
-    peak = sms * 128 * clk      # FP32 lane-operations per second (nominal: 128 lanes per SM, max clock)
-    out["residual_df"] = {"bound": "fp32 pipe", "n": n, "nrhs": R, "ms": ms,
-                          "complex_macs_per_s": macs / (ms * 1e-3),
-                          "fp32_ops_per_s": ops / (ms * 1e-3), "peak_fp32_ops_per_s": peak,
-                          "frac": ops / (ms * 1e-3) / peak,
-                          "peak_source": "nominal: SMs x 128 FP32 lanes x 2.07 GHz; ~52 FP32 operations per "
-                                         "double-float complex multiply-add"}
-    del Mdf
-    prob = W.cfg1()
-    pts = prob.points.to(dev)
-    coef = prob.alpha * prob.k0 ** 2
-    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
-    (M32,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("c64",))
-    ts = []
-    for rep in range(4):
-        A = torch.empty_strided(M32.size(), M32.stride(), dtype=M32.dtype, device=dev)
-        A.copy_(M32)
-        torch.cuda.synchronize()
-        e0.record()
-        E.lu_factor(A, check_singular=False)
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
-    lu_ms = min(ts[1:])
-    out["lu_panel"] = {"bound": "latency (one cross-CTA pivot exchange per column)", "n": prob.n,
-                       "lu_ms": lu_ms, "us_per_column": 1e3 * lu_ms / prob.n,
-                       "note": "complex64 LU of order 2000: panels in one thread-block cluster; the "
-                               "trailing update is under 10% of it"}
-    return out
+            "corrections_after_graph": extra_total, "refactored_with_partial_pivoting": refactored}
 
 
 def run_ours(args, rank, world, local):

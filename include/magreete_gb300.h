@@ -104,6 +104,41 @@ int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm,
                   void* work, size_t work_bytes, void* stream);
 
 /*
+ * Options of one factorisation (no counterpart in the reference, whose LU is
+ * LAPACK's): the choices the process-wide MGT_TUNE_* keys set, per call, so
+ * that concurrent callers (a server and a batched sweep in one process) do
+ * not change each other's factorisations.  Zero / negative fields take the
+ * process-wide value (mgt_set_tuning).
+ *   pivoting  MGT_PIVOT_PARTIAL: LAPACK's partial pivoting (largest |re|+|im|
+ *             of the column, lowest row on ties; the reference's pivot
+ *             sequence).  MGT_PIVOT_TILE (complex64 only): each 64-column
+ *             panel chooses its pivots among the 64 rows of its diagonal
+ *             tile; the rows below are solved against the tile's U
+ *             (L21 = A21 U11^-1), so no panel needs any exchange between
+ *             CTAs.  P A = L U still holds; the growth of the factors is not
+ *             bounded like partial pivoting's, so it is meant for the mixed
+ *             method, whose refinement certifies the solution (callers fall
+ *             back to partial pivoting when it does not converge).  An exact
+ *             zero tile pivot sets info as a zero pivot does.
+ *   panel_rows, panel_max_ctas, cooperative, lookahead, outer_block: as the
+ *             MGT_TUNE_* keys of the same names (cooperative / lookahead: -1 =
+ *             process value; outer_block 64 or 128)
+ */
+#define MGT_PIVOT_PARTIAL 0
+#define MGT_PIVOT_TILE 1
+typedef struct mgt_lu_options {
+  int32_t size;            /* sizeof(mgt_lu_options) */
+  int32_t pivoting;
+  int32_t panel_rows;
+  int32_t panel_max_ctas;
+  int32_t cooperative;
+  int32_t lookahead;
+  int32_t outer_block;
+} mgt_lu_options;
+int mgt_lu_factor_ex(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, void* work, size_t work_bytes,
+                     const mgt_lu_options* options, void* stream);
+
+/*
  * mgt_lu_factor without a workspace argument; no counterpart in the
  * reference (whose solve is a single torch.linalg.solve call on the CPU).
  * For callers that cannot obtain device memory at call time -- a C or

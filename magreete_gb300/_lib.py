@@ -33,6 +33,19 @@ MGT_TUNE_FUSED_RIGHT = 8
 MGT_TUNE_PANEL_CLUSTER = 9
 MGT_TUNE_SYM_ASSEMBLY = 10
 MGT_TC_TF32X3, MGT_TC_F16X2 = 0, 1
+MGT_PIVOT_PARTIAL, MGT_PIVOT_TILE = 0, 1
+
+class LuOptions(ctypes.Structure):
+    """mgt_lu_options: per-call choices of one LU factorisation (zero / -1
+    fields take the process-wide tuning values)."""
+    _fields_ = [("size", ctypes.c_int32), ("pivoting", ctypes.c_int32), ("panel_rows", ctypes.c_int32),
+                ("panel_max_ctas", ctypes.c_int32), ("cooperative", ctypes.c_int32), ("lookahead", ctypes.c_int32),
+                ("outer_block", ctypes.c_int32)]
+
+    def __init__(self, pivoting=0, panel_rows=0, panel_max_ctas=0, cooperative=-1, lookahead=-1, outer_block=0):
+        super().__init__(ctypes.sizeof(LuOptions), pivoting, panel_rows, panel_max_ctas, cooperative, lookahead,
+                         outer_block)
+
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -50,6 +63,7 @@ SIGNATURES = {
     "mgt_lu_workspace_bytes": (_i32, [_i32, _i64, ctypes.POINTER(_sz)]),
     "mgt_lu_factor": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _sz, _vp]),
     "mgt_lu_factor_static": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _vp]),
+    "mgt_lu_factor_ex": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _sz, ctypes.POINTER(LuOptions), _vp]),
     "mgt_lu_solve_workspace_bytes": (_i32, [_i32, _i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_lu_solve": (_i32, [_i32, _vp, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_workspace_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int32), _vp]),

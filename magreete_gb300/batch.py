@@ -4,15 +4,23 @@ A sweep over disorder realisations or frequencies (the driver's per-copy and
 per-k0 loops, magreete.py:114, :371) is a set of independent requests.  A
 ``BatchedSweep`` groups them, preallocates every device buffer of a group,
 and captures the whole group -- assembly, complex64 LU, refined solve (one
-correction) and the final residual norms -- into one CUDA
-graph whose instances run as concurrent branches on `branches` streams.  One
+correction) and the final residual norms -- into one CUDA graph whose
+instances run as concurrent branches on `branches` streams.  One
 ``replay()`` then launches the group.  Instances whose certified relative
 residual is still above the tolerance after the graph get further
-corrections outside it.
+corrections outside it, and, if those do not reach it either, a fresh
+factorisation with partial pivoting.
+
+Every factorisation carries its own options (``_lib.LuOptions``): nothing
+here changes the library's process-wide tuning, so a sweep and a server in
+one process do not affect each other.  With tile pivoting (the default) the
+LU has no spin-waits between CTAs at all; with partial pivoting the panels
+launch without the cooperative attribute (capturable) and each is limited to
+its share of the SMs.
 
 The autotuner (``autotune``) times the group's graph for a few settings of
-the concurrent-branch count and of the LU's panel height (rows per CTA of the
-panel kernel), keeps the fastest, and caches the choice per size bucket.
+the concurrent-branch count, the pivoting and the LU's outer block width,
+keeps the fastest, and caches the choice per size bucket.
 """
 from __future__ import annotations
 
@@ -39,8 +47,9 @@ def _ptr(t):
 class _Instance:
     """Device buffers of one request of a batch."""
 
-    def __init__(self, prob, dev, lib):
+    def __init__(self, prob, dev, lib, lu_options):
         self.prob = prob
+        self.lu_options = lu_options
         n, R = prob.n, prob.nrhs
         self.pts = prob.points.to(dev)
         ld = (n + 15) // 16 * 16
@@ -66,7 +75,7 @@ class _Instance:
         return sum(t.numel() * t.element_size() for t in (self.M32, self.Mdf, self.luw, self.rw, self.B, self.X)) + \
             self.M32.shape[0] * 16 * 8
 
-    def enqueue(self, lib, stream_ptr, corrections=1):
+    def enqueue(self, lib, stream_ptr, corrections=1, options=None):
         """Stream-ordered solve: assembly, LU, refined solve, norms."""
         p = self.prob
         n, R = p.n, p.nrhs
@@ -75,8 +84,10 @@ class _Instance:
         L.check(lib.mgt_assemble_system(E.KIND_CODE[p.kind], _ptr(self.pts), p.N, float(p.k0), coef.real, coef.imag,
                                         shift.real, shift.imag, _ptr(self.Mdf), n, L.MGT_CDF, _ptr(self.M32),
                                         self.M32.stride(0), L.MGT_C64, stream_ptr), "mgt_assemble_system")
-        L.check(lib.mgt_lu_factor(L.MGT_C64, _ptr(self.M32), n, self.M32.stride(0), _ptr(self.perm), _ptr(self.luw),
-                                  self.luw.numel(), stream_ptr), "mgt_lu_factor")
+        opt = options if options is not None else self.lu_options
+        L.check(lib.mgt_lu_factor_ex(L.MGT_C64, _ptr(self.M32), n, self.M32.stride(0), _ptr(self.perm),
+                                     _ptr(self.luw), self.luw.numel(), ctypes.byref(opt), stream_ptr),
+                "mgt_lu_factor_ex")
         L.check(lib.mgt_refine_start(_ptr(self.M32), self.M32.stride(0), _ptr(self.perm), n, _ptr(self.B), R,
                                      _ptr(self.X), R, R, _ptr(self.rw), self.rw.numel(), stream_ptr),
                 "mgt_refine_start")
@@ -106,34 +117,38 @@ class _Instance:
 class BatchedSweep:
     """One CUDA graph for a group of independent refined solves.
 
-    problems: workloads.Problem list (any kinds / sizes)
-    branches: concurrent graph branches (streams) the instances are spread over
+    problems:    workloads.Problem list (any kinds / sizes)
+    branches:    concurrent graph branches (streams) the instances are spread over
+    pivoting:    "tile" (default) or "partial" (see engine.lu_factor)
+    outer_block: 128 (default) or 64, the complex64 LU's outer block width
+    panel_rows:  rows per CTA of partial-pivoting panels (0: library default)
     """
 
-    def __init__(self, problems, branches=8, tol=E.DEFAULT_TOL, device=None):
+    def __init__(self, problems, branches=8, tol=E.DEFAULT_TOL, device=None, pivoting="tile", outer_block=128,
+                 panel_rows=0):
         self.lib = L.load()
         self.dev = device or torch.device("cuda", torch.cuda.current_device())
         self.tol = tol
-        # a panel CTA holds at most 220 KB of rows (complex64, 64 columns): the
-        # largest instance needs ceil(8 n / 440) CTAs; keep the panels of all
-        # branches within the SM count
+        self.pivoting = pivoting
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
-        need = max(1, math.ceil(max(p.n for p in problems) / 440))
-        self.branches = max(1, min(int(branches), sms // need))
+        if pivoting == "partial":
+            # a panel CTA holds at most 220 KB of rows (complex64, 64 columns): the
+            # largest instance needs ceil(8 n / 440) CTAs; keep the panels of all
+            # branches within the SM count, so that no panel waits on another
+            need = max(1, math.ceil(max(p.n for p in problems) / 440))
+            self.branches = max(1, min(int(branches), sms // need))
+        else:
+            self.branches = max(1, int(branches))
+        # launched without the cooperative attribute (capturable), no lookahead (capture)
+        self.lu_options = L.LuOptions(pivoting=E.PIVOTING[pivoting], panel_rows=int(panel_rows),
+                                      panel_max_ctas=max(1, sms // self.branches), cooperative=0, lookahead=0,
+                                      outer_block=int(outer_block))
         # largest first, so that the long solves start early in every branch
         order = sorted(range(len(problems)), key=lambda i: -problems[i].n)
         self.order = order
-        self.inst = [_Instance(problems[i], self.dev, self.lib) for i in order]
+        self.inst = [_Instance(problems[i], self.dev, self.lib, self.lu_options) for i in order]
         self.graph = None
-
-    def _graph_mode(self, on):
-        """Panels launched without the cooperative attribute (capturable), each
-        limited to its share of the SMs so that the panels of all branches fit
-        on the GPU at once."""
-        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
-        L.check(self.lib.mgt_set_tuning(L.MGT_TUNE_COOPERATIVE, 0 if on else 1), "mgt_set_tuning")
-        L.check(self.lib.mgt_set_tuning(L.MGT_TUNE_PANEL_MAX_CTAS, max(1, sms // self.branches) if on else 0),
-                "mgt_set_tuning")
+        self.refactored = 0
 
     def _enqueue_all(self):
         main = torch.cuda.current_stream()
@@ -149,21 +164,13 @@ class BatchedSweep:
 
     def warmup(self):
         """One eager run (initialises kernels' one-time attributes; required before capture)."""
-        self._graph_mode(True)
-        try:
-            self._enqueue_all()
-            torch.cuda.synchronize(self.dev)
-        finally:
-            self._graph_mode(False)
+        self._enqueue_all()
+        torch.cuda.synchronize(self.dev)
 
     def capture(self):
         self.graph = torch.cuda.CUDAGraph()
-        self._graph_mode(True)
-        try:
-            with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
-                self._enqueue_all()
-        finally:
-            self._graph_mode(False)
+        with torch.cuda.graph(self.graph, capture_error_mode="thread_local"):
+            self._enqueue_all()
         return self
 
     def replay(self):
@@ -180,8 +187,24 @@ class BatchedSweep:
                 inst.correct(self.lib, sp)
                 inst.measure(self.lib, sp)
                 torch.cuda.synchronize(self.dev)
-                rr = inst.rel_residual()
+                nr = inst.rel_residual()
                 k += 1
+                if not nr < 0.9 * rr:
+                    rr = nr
+                    break
+                rr = nr
+            if not rr <= self.tol:
+                # the refinement cannot use these factors: partial pivoting, eagerly
+                inst.enqueue(self.lib, sp, corrections=1, options=L.LuOptions(pivoting=L.MGT_PIVOT_PARTIAL))
+                torch.cuda.synchronize(self.dev)
+                rr = inst.rel_residual()
+                while rr > self.tol and k < 2 * E.DEFAULT_MAX_ITER:
+                    inst.correct(self.lib, sp)
+                    inst.measure(self.lib, sp)
+                    torch.cuda.synchronize(self.dev)
+                    rr = inst.rel_residual()
+                    k += 1
+                self.refactored += 1
             extra.append(k)
             res.append(rr)
         return extra, res
@@ -199,38 +222,35 @@ def _bucket(problems):
     return f"n<={2 ** math.ceil(math.log2(max(n, 2)))}"
 
 
-def autotune(problems, branch_options=(4, 8, 16), panel_rows_options=(128, 256, 512), reps=1, cache=TUNE_CACHE):
-    """Pick (branches, panel rows per CTA) for groups like `problems` by timing
-    graph replays; the choice is cached per size bucket.  Returns the dict."""
-    lib = L.load()
+def autotune(problems, branch_options=(4, 8, 16), pivoting_options=("tile", "partial"), outer_options=(128, 64),
+             reps=1, cache=TUNE_CACHE):
+    """Pick (branches, pivoting, outer block width) for groups like `problems`
+    by timing graph replays; the choice is cached per size bucket.  Returns
+    the dict (keyword arguments of BatchedSweep plus the timings)."""
     key = _bucket(problems)
     try:
         with open(cache) as f:
             table = json.load(f)
     except (OSError, ValueError):
         table = {}
-    if key in table:
-        best = table[key]
-        lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(best["panel_rows"]))
-        return best
+    if key in table and {"branches", "pivoting", "outer_block"} <= set(table[key]):
+        return table[key]
     results = []
-    for rows in panel_rows_options:
-        L.check(lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(rows)), "mgt_set_tuning")
-        for br in branch_options:
-            sw = BatchedSweep(problems, branches=br)
-            sw.warmup()
-            sw.capture()
-            sw.replay()
-            t0 = time.perf_counter()
-            for _ in range(reps):
+    for piv in pivoting_options:
+        for ob in outer_options:
+            for br in branch_options:
+                sw = BatchedSweep(problems, branches=br, pivoting=piv, outer_block=ob)
+                sw.warmup()
+                sw.capture()
                 sw.replay()
-            dt = (time.perf_counter() - t0) / reps
-            results.append({"panel_rows": rows, "branches": br, "seconds": dt})
-            del sw
-            torch.cuda.empty_cache()
-    best = min(results, key=lambda r: r["seconds"])
-    lib.mgt_set_tuning(L.MGT_TUNE_PANEL_ROWS, int(best["panel_rows"]))
-    best = dict(best, candidates=results)
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    sw.replay()
+                dt = (time.perf_counter() - t0) / reps
+                results.append({"pivoting": piv, "outer_block": ob, "branches": br, "seconds": dt})
+                del sw
+                torch.cuda.empty_cache()
+    best = dict(min(results, key=lambda r: r["seconds"]), candidates=results)
     table[key] = best
     try:
         os.makedirs(os.path.dirname(cache), exist_ok=True)

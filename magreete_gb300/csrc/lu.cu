@@ -42,11 +42,13 @@ struct LuWsLayout {
   size_t slots = 64;      // 2 sets x 2*NBmax x int2 (pos, src)
   size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
   size_t inv;             // 2 x NBmax x NBmax complex: inverses of a 128-wide block's diagonal blocks
+  size_t uinv;            // NBmax x NBmax complex64: U11^-1 of the last tile-pivoting panel
   size_t total;
   LuWsLayout() {
     records = (slots + 2 * 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
     inv = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
-    total = inv + 2 * (size_t)kNBmax * kNBmax * sizeof(double2);
+    uinv = inv + 2 * (size_t)kNBmax * kNBmax * sizeof(double2);
+    total = uinv + (size_t)kNBmax * kNBmax * sizeof(float2);
   }
 };
 
@@ -1201,6 +1203,191 @@ static int trailing_update(const TcLU* tc, int M, int N, int K, const float2* A,
 
 static std::atomic<int> g_panel_cluster{1};     // complex64 panels of <= 16 CTAs as one cluster
 
+// Options of one factorisation: the process-wide tuning values, overridden
+// by the caller's mgt_lu_options where given.
+struct LuOpts {
+  int pivoting = MGT_PIVOT_PARTIAL;
+  int panel_rows, outer_block, panel_max_ctas, cooperative, panel_reg, lookahead, fused_right, panel_cluster;
+  LuOpts() {
+    panel_rows = g_panel_rows.load(std::memory_order_relaxed);
+    outer_block = g_outer_block.load(std::memory_order_relaxed);
+    panel_max_ctas = g_panel_max_ctas.load(std::memory_order_relaxed);
+    cooperative = g_cooperative.load(std::memory_order_relaxed);
+    panel_reg = g_panel_reg.load(std::memory_order_relaxed);
+    lookahead = g_lookahead.load(std::memory_order_relaxed);
+    fused_right = g_fused_right.load(std::memory_order_relaxed);
+    panel_cluster = g_panel_cluster.load(std::memory_order_relaxed);
+  }
+};
+
+static int resolve_lu_options(const mgt_lu_options* o, LuOpts* r) {
+  if (!o) return MGT_OK;
+  if (o->size < (int32_t)sizeof(mgt_lu_options)) return MGT_ERR_ARG;
+  if (o->pivoting != MGT_PIVOT_PARTIAL && o->pivoting != MGT_PIVOT_TILE) return MGT_ERR_ARG;
+  r->pivoting = o->pivoting;
+  if (o->panel_rows > 0) {
+    if (o->panel_rows < 32 || o->panel_rows > 4096) return MGT_ERR_ARG;
+    r->panel_rows = o->panel_rows;
+  }
+  if (o->panel_max_ctas > 0) r->panel_max_ctas = std::min(o->panel_max_ctas, 4096);
+  if (o->cooperative >= 0) r->cooperative = o->cooperative ? 1 : 0;
+  if (o->lookahead >= 0) r->lookahead = o->lookahead ? 1 : 0;
+  if (o->outer_block > 0) {
+    if (o->outer_block != 64 && o->outer_block != 128) return MGT_ERR_ARG;
+    r->outer_block = o->outer_block;
+  }
+  return MGT_OK;
+}
+
+// ---------------------------------------------------------------- tile-pivoting panel (complex64)
+//
+// MGT_PIVOT_TILE: the pivots of a 64-column panel are chosen among the rows
+// of its diagonal tile.  lu_tile_kernel (one CTA) factors the w x w tile with
+// partial pivoting among the tile's rows, records the interchanges in the slot
+// format of the panel kernels (the swap kernels then apply them to the other
+// columns) and in perm, and writes U11^-1; lu_l21_kernel solves every row below
+// the tile, L21 = A21 U11^-1, with no exchange between CTAs.  The system
+// matrices of this engine rarely need a pivot from outside the tile (LAPACK
+// swaps a few rows in a thousand there); the growth that remains is what
+// iterative refinement absorbs.
+constexpr int kTileLD = 65;   // padded row stride of the tile in shared memory
+
+__global__ void __launch_bounds__(256)
+lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __restrict__ perm, PanelWs ws,
+               float2* __restrict__ Uinv) {
+  // A: the tile's top-left element (row j0, column j0); w <= 64
+  __shared__ float2 T[64 * kTileLD];
+  __shared__ float2 col[64];
+  __shared__ int s_piv[64];
+  __shared__ int s_p;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < w * w; idx += 256) {
+    const int i = idx / w, k = idx - i * w;
+    T[i * kTileLD + k] = A[(int64_t)i * lda + k];
+  }
+  if (tid < 64) s_piv[tid] = tid;
+  __syncthreads();
+  for (int c = 0; c < w; ++c) {
+    if (warp == 0) {
+      // largest |re| + |im| among rows c .. w-1 of column c, lowest row on ties
+      uint32_t best = 0;
+      int bi = w;
+      for (int i = c + lane; i < w; i += 32) {
+        const float2 v = T[i * kTileLD + c];
+        const uint32_t key = __float_as_uint(fabsf(v.x) + fabsf(v.y));
+        if (bi == w || key > best) { best = key; bi = i; }
+      }
+      const uint32_t mx = __reduce_max_sync(0xffffffffu, best);
+      const int p = (int)__reduce_min_sync(0xffffffffu, (uint32_t)((bi < w && best == mx) ? bi : w));
+      if (lane == 0) s_p = p < w ? p : c;
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != c) {
+      for (int k = tid; k < w; k += 256) {
+        const float2 t = T[c * kTileLD + k];
+        T[c * kTileLD + k] = T[p * kTileLD + k];
+        T[p * kTileLD + k] = t;
+      }
+      if (tid == 0) {
+        const int t = s_piv[c];
+        s_piv[c] = s_piv[p];
+        s_piv[p] = t;
+      }
+    }
+    __syncthreads();
+    const float2 piv = T[c * kTileLD + c];
+    if (piv.x == 0.f && piv.y == 0.f) {
+      // an exact zero pivot: recorded like LAPACK's info; the column stays as it is
+      if (tid == 0 && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
+    } else {
+      const float2 rp = crecip(piv);
+      for (int i = c + 1 + tid; i < w; i += 256) T[i * kTileLD + c] = cmul(T[i * kTileLD + c], rp);
+      __syncthreads();
+      const int rem = w - c - 1;
+      for (int idx = tid; idx < rem * rem; idx += 256) {
+        const int i = c + 1 + idx / rem, k = c + 1 + idx % rem;
+        cfms(T[i * kTileLD + k], T[i * kTileLD + c], T[c * kTileLD + k]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < w * w; idx += 256) {
+    const int i = idx / w, k = idx - i * w;
+    A[(int64_t)i * lda + k] = T[i * kTileLD + k];
+  }
+  if (warp == 0) {
+    // interchanges: position q of the tile holds the row that started at s_piv[q]
+    for (int q = lane; q < kNBmax; q += 32) ws.slots[q] = make_int2(q, q < w ? s_piv[q] : q);
+    if (lane == 0) *ws.nslot = kNBmax;
+    int32_t pv[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int q = lane + 32 * j;
+      if (q < w) pv[j] = perm[j0 + s_piv[q]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int q = lane + 32 * j;
+      if (q < w) perm[j0 + q] = pv[j];
+    }
+  }
+  __syncthreads();
+  // U11^-1 in place in the upper triangle of T, one column j at a time:
+  // x = U[0:j, j];  x <- -Uinv[0:j, 0:j] x / U[j][j]  (columns left of j are
+  // already inverted), then the diagonal
+  for (int j = 0; j < w; ++j) {
+    const float2 ujj = T[j * kTileLD + j];
+    const bool nz = ujj.x != 0.f || ujj.y != 0.f;
+    const float2 rj = nz ? crecip(ujj) : make_float2(0.f, 0.f);
+    if (tid < j) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int k = tid; k < j; ++k) cfma(acc, T[tid * kTileLD + k], T[k * kTileLD + j]);
+      col[tid] = cmul(acc, make_float2(-rj.x, -rj.y));
+    }
+    __syncthreads();
+    if (tid < j) T[tid * kTileLD + j] = col[tid];
+    if (tid == 0) T[j * kTileLD + j] = rj;
+    __syncthreads();
+  }
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int i = idx >> 6, k = idx & 63;
+    Uinv[idx] = (i < w && k < w && k >= i) ? T[i * kTileLD + k] : make_float2(0.f, 0.f);
+  }
+}
+
+// Rows below the tile: A21 <- A21 U11^-1 (w columns), 32 rows per CTA.
+__global__ void __launch_bounds__(256)
+lu_l21_kernel(float2* __restrict__ A, int64_t lda, int rows, int w, const float2* __restrict__ Uinv) {
+  // A: first row below the tile, first column of the panel
+  __shared__ float2 Ui[64 * 64];
+  __shared__ float2 Ar[32 * 64];
+  const int tid = threadIdx.x, r0 = blockIdx.x * 32;
+  for (int idx = tid; idx < 64 * 64; idx += 256) Ui[idx] = Uinv[idx];
+  for (int idx = tid; idx < 32 * 64; idx += 256) {
+    const int r = idx >> 6, k = idx & 63;
+    Ar[idx] = (r0 + r < rows && k < w) ? A[(int64_t)(r0 + r) * lda + k] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int r = tid >> 3, g = tid & 7;
+  float2 acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = make_float2(0.f, 0.f);
+  for (int i = 0; i < w; ++i) {
+    const float2 a = Ar[r * 64 + i];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cfma(acc[q], a, Ui[i * 64 + g + 8 * q]);
+  }
+  if (r0 + r < rows) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = g + 8 * q;
+      if (k < w) A[(int64_t)(r0 + r) * lda + k] = acc[q];
+    }
+  }
+}
+
 // Largest cluster of register panel CTAs the device schedules (16, 8 or 0).
 static int cluster_panel_max() {
   static int cmax_dev[kMaxDevices];
@@ -1262,7 +1449,7 @@ static SideStream* side_stream() {
 
 template <typename T, int NB>
 static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* work, cudaStream_t s,
-                          const TcLU* tc = nullptr) {
+                          const LuOpts& opt, const TcLU* tc = nullptr) {
   using V = cplx<T>;
   static OncePerDevice once;
   once([] {
@@ -1281,13 +1468,26 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   // CTAs of the panel kernel for a panel of m rows
   auto panel_ctas = [&](int m) -> int {
     const int64_t min_g_smem = ((int64_t)m * NB * (int64_t)sizeof(V) + kPanelSmemBudget - 1) / kPanelSmemBudget;
-    const int rows_target = g_panel_rows.load(std::memory_order_relaxed);
+    const int rows_target = opt.panel_rows;
     int G = (int)std::max<int64_t>({1, (m + rows_target - 1) / rows_target, min_g_smem});
-    const int gmax = g_panel_max_ctas.load(std::memory_order_relaxed);
+    const int gmax = opt.panel_max_ctas;
     return std::min(G, gmax > 0 ? std::min(gmax, sms) : sms);
   };
   // factor columns [j0, j0+w) over rows [j0, n); the interchanges go to slot set `set`
   auto panel_only = [&](int j0, int w, int set) -> int {
+    if constexpr (sizeof(T) == 4) {
+      if (opt.pivoting == MGT_PIVOT_TILE) {
+        float2* Ui = reinterpret_cast<float2*>((char*)work + LuWsLayout().uinv);
+        lu_tile_kernel<<<1, 256, 0, s>>>(A + (int64_t)j0 * lda + j0, lda, w, j0, perm, panel_ws(work, set), Ui);
+        count_launch();
+        const int below = n - j0 - w;
+        if (below > 0) {
+          lu_l21_kernel<<<(below + 31) / 32, 256, 0, s>>>(A + (int64_t)(j0 + w) * lda + j0, lda, below, w, Ui);
+          count_launch();
+        }
+        return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+      }
+    }
     const int m = n - j0;
     const int G = panel_ctas(m);
     int rpc = (m + G - 1) / G;
@@ -1306,15 +1506,15 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     cfg.attrs = attr;
     // Without the attribute (CUDA-graph capture of concurrent branches) the
     // caller keeps the panels' total CTA count within the SM count instead.
-    cfg.numAttrs = g_cooperative.load(std::memory_order_relaxed) ? 1 : 0;
+    cfg.numAttrs = opt.cooperative ? 1 : 0;
     // up to one row per thread: the register-resident kernel, as one thread-
     // block cluster (exchange in distributed shared memory) when it fits
     cudaError_t le;
-    const int reg_mode = g_panel_reg.load(std::memory_order_relaxed);
+    const int reg_mode = opt.panel_reg;
     bool launched = false;
     if constexpr (sizeof(T) == 4) {
       const int cmax = cluster_panel_max();
-      if (rpc <= kPanelThreads && reg_mode != 0 && G <= cmax && g_panel_cluster.load(std::memory_order_relaxed)) {
+      if (rpc <= kPanelThreads && reg_mode != 0 && G <= cmax && opt.panel_cluster) {
         cudaLaunchConfig_t cc = cfg;
         cudaLaunchAttribute ca[1];
         ca[0].id = cudaLaunchAttributeClusterDimension;
@@ -1379,7 +1579,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   auto update = [&](int r0, int c0, int k0, int K, int rows, int cols, bool dominant) -> int {
     return update_on(s, r0, c0, k0, K, rows, cols, dominant, 0);
   };
-  if (tc == nullptr || g_outer_block.load(std::memory_order_relaxed) == NB) {
+  if (tc == nullptr || opt.outer_block == NB) {
     for (int j0 = 0; j0 < n; j0 += NB) {
       const int w = std::min(NB, n - j0);
       int e = panel_step(j0, w, 1);
@@ -1408,8 +1608,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);
   SideStream* side = nullptr;
-  if (g_lookahead.load(std::memory_order_relaxed) && g_cooperative.load(std::memory_order_relaxed) &&
-      cap == cudaStreamCaptureStatusNone)
+  if (opt.lookahead && (opt.cooperative || opt.pivoting == MGT_PIVOT_TILE) && cap == cudaStreamCaptureStatusNone)
     side = side_stream();
   // the two inner panels of the block at J0 and everything up to (not
   // including) the columns at or right of `far`: interchanges on the left,
@@ -1434,7 +1633,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     const int right = n - J0 - W;
     if (right <= 0) return;
     if constexpr (sizeof(T) == 4) {
-      if (wb > 0 && g_fused_right.load(std::memory_order_relaxed)) {
+      if (wb > 0 && opt.fused_right) {
         V* Inv = reinterpret_cast<V*>((char*)work + LuWsLayout().inv);
         lower_block_inverses<T>(A + (int64_t)J0 * lda + J0, lda, W, Inv, s);
         lu_block_right_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, block_right_smem<NB>(sizeof(V)), s>>>(
@@ -1466,7 +1665,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       if (cudaEventRecord(side->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, side->fork, 0) != cudaSuccess)
         return MGT_ERR_CUDA;
       dom_begin(s2);
-      e = tc_gemm(tc->plan, tc->cmap, M, rest, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - panel_ctas(M)));
+      const int reserve = opt.pivoting == MGT_PIVOT_TILE ? 16 : panel_ctas(M);
+      e = tc_gemm(tc->plan, tc->cmap, M, rest, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - reserve));
       dom_end(s2, 8.0 * M * (double)rest * W, sizeof(V) * (2.0 * M * (double)rest + (double)W * rest));
       // once forked, the join is recorded whatever happened
       const bool joined = cudaEventRecord(side->join, s2) == cudaSuccess;
@@ -1491,9 +1691,10 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     // inner panels at ~4.5 us per column plus their interchanges)
     bool overlap = side != nullptr && rest > 0;
     if (overlap) {
-      const int G = panel_ctas(n - P0);
+      const bool tile = opt.pivoting == MGT_PIVOT_TILE;
+      const int G = tile ? 16 : panel_ctas(n - P0);
       const double t_upd = 8.0 * (n - P0) * (double)rest * W / 2.5e14;
-      const double t_pan = 2.0 * NB * 4.5e-6 + 1e-4;
+      const double t_pan = tile ? 2 * 40e-6 + 1e-4 : 2.0 * NB * 4.5e-6 + 1e-4;
       overlap = sms - G >= 16 && std::max(t_upd * sms / (sms - G), t_pan) < t_upd + t_pan;
     }
     if (!overlap) {
@@ -1654,24 +1855,35 @@ extern "C" int mgt_lu_workspace_bytes(int dtype, int64_t n, size_t* bytes) {
   return MGT_OK;
 }
 
-extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, void* work,
-                             size_t work_bytes, void* stream) {
+extern "C" int mgt_lu_factor_ex(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, void* work,
+                                size_t work_bytes, const mgt_lu_options* options, void* stream) {
   if (!A || !perm || !work || n <= 0 || lda < n || n > (1 << 20)) return MGT_ERR_ARG;
   if (work_bytes < LuWsLayout().total) return MGT_ERR_WORKSPACE;
+  LuOpts opt;
+  int e = resolve_lu_options(options, &opt);
+  if (e != MGT_OK) return e;
   cudaStream_t s = (cudaStream_t)stream;
-  if (dtype == MGT_C128) return lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s);
+  if (dtype == MGT_C128) {
+    if (opt.pivoting != MGT_PIVOT_PARTIAL) return MGT_ERR_UNSUPPORTED;
+    return lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s, opt);
+  }
   if (dtype == MGT_C64) {
     // tensor-core trailing update when the workspace holds its split buffers,
     // the rows are 16-byte aligned (even lda) and the driver exposes TMA maps
     if (n >= kTcMinN && (lda & 1) == 0 && work_bytes >= tc_region_offset() + tc_scratch_bytes(n) && tc_available()) {
       TcLU tc;
-      int e = tc.plan.init((char*)work + tc_region_offset(), n);
+      e = tc.plan.init((char*)work + tc_region_offset(), n);
       if (e == MGT_OK) e = tc_make_cmap(&tc.cmap, (float2*)A, n, n, lda);
-      if (e == MGT_OK) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, &tc);
+      if (e == MGT_OK) return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, opt, &tc);
     }
-    return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+    return lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, opt);
   }
   return MGT_ERR_ARG;
+}
+
+extern "C" int mgt_lu_factor(int dtype, void* A, int64_t n, int64_t lda, int32_t* perm, void* work,
+                             size_t work_bytes, void* stream) {
+  return mgt_lu_factor_ex(dtype, A, n, lda, perm, work, work_bytes, nullptr, stream);
 }
 
 extern "C" int mgt_lu_solve_workspace_bytes(int dtype, int64_t n, int64_t nrhs, size_t* bytes) {
@@ -1759,8 +1971,9 @@ extern "C" int mgt_lu_factor_static(int dtype, void* A, int64_t n, int64_t lda, 
   int e = static_lu_scratch(&work);
   if (e != MGT_OK) return e;
   cudaStream_t s = (cudaStream_t)stream;
-  e = dtype == MGT_C128 ? lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s)
-                        : lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s);
+  const LuOpts opt;
+  e = dtype == MGT_C128 ? lu_factor_impl<double, 32>((double2*)A, (int)n, lda, perm, work, s, opt)
+                        : lu_factor_impl<float, 64>((float2*)A, (int)n, lda, perm, work, s, opt);
   if (e != MGT_OK) return e;
   if (info) {
     LuWsLayout L;

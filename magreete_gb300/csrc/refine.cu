@@ -12,6 +12,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "diag.cuh"
+#include "residual_tc.cuh"
 
 namespace mgt {
 
@@ -275,31 +276,65 @@ static int residual_impl(const float4* M, int64_t ldm, const double2* X, int64_t
 
 size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem);
 
-// refinement workspace layout
+// refinement workspace layout: the residual runs on the tensor cores
+// (residual_tc.cu) where the device and shape allow, in double-float on the
+// FP32 pipes otherwise
 struct RefineWs {
-  float4* Xs;     // n x nrhs double-float copy of X
+  bool tc;        // tensor-core residual
+  float4* Xs;     // (double-float residual) n x nrhs double-float copy of X
   double2* Rr;    // n x nrhs residual
   float2* R32;    // n x nrhs complex64 residual / right-hand side
   float2* D32;    // n x nrhs complex64 correction
   double* norms;  // [0] = ||B||^2, [1] = ||R||^2
   void* tri;      // triangular-solve flags
-  double2* part;  // split-K partial sums of the residual
+  double2* part;  // (double-float residual) split-K partial sums
   int64_t part_elems;
+  int* rowexp;    // (tensor-core residual) row exponents of M
+  void* tcw;      // (tensor-core residual) its workspace
+  size_t tcw_bytes;
   size_t total;
   RefineWs(void* base, int64_t n, int64_t r) {
     char* b = (char*)base;
     size_t off = 0;
     auto take = [&](size_t bytes) { char* p = b ? b + off : nullptr; off += (bytes + 255) & ~size_t(255); return p; };
-    Xs = (float4*)take(n * r * sizeof(float4));
+    tc = residual_tc_supported(n, n, r);
     Rr = (double2*)take(n * r * sizeof(double2));
     R32 = (float2*)take(n * r * sizeof(float2));
     D32 = (float2*)take(n * r * sizeof(float2));
     norms = (double*)take(2 * sizeof(double));
     tri = take(tri_solve_workspace_bytes(n, r, sizeof(float2)));
-    part_elems = residual_partial_elems(n, n, r);
-    part = (double2*)take(part_elems * sizeof(double2));
+    Xs = nullptr;
+    part = nullptr;
+    part_elems = 0;
+    rowexp = nullptr;
+    tcw = nullptr;
+    tcw_bytes = 0;
+    if (tc) {
+      rowexp = (int*)take(n * sizeof(int));
+      off = (off + 1023) & ~size_t(1023);
+      tcw_bytes = residual_tc_workspace_bytes(n, n, r);
+      tcw = take(tcw_bytes);
+    } else {
+      Xs = (float4*)take(n * r * sizeof(float4));
+      part_elems = residual_partial_elems(n, n, r);
+      part = (double2*)take(part_elems * sizeof(double2));
+    }
     total = off;
   }
+  // Rr = B - M X; rowexp_ready: the row exponents of this M are in rowexp
+  int residual(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb, int n,
+               int nr, bool rowexp_ready, cudaStream_t s) {
+    if (tc) {
+      if (!rowexp_ready) {
+        int e = residual_tc_rowexp(M, ldm, n, n, rowexp, s);
+        if (e != MGT_OK) return e;
+      }
+      return residual_tc(M, ldm, n, n, X, ldx, nr, B, ldb, Rr, nr, rowexp, tcw, tcw_bytes, s);
+    }
+    return residual_impl(M, ldm, X, ldx, B, ldb, Rr, nr, n, nr, Xs, part, part_elems, s);
+  }
+  // device status word of the tensor-core residual (MGT_OK or MGT_ERR_TIMEOUT), or null
+  int* status() const { return tc ? (int*)tcw : nullptr; }
 };
 
 }  // namespace mgt
@@ -312,8 +347,9 @@ extern "C" int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, c
 
 extern "C" int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {
   if (!bytes || n <= 0 || nrhs <= 0) return MGT_ERR_ARG;
-  *bytes = (((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255)) +
-           residual_partial_elems(n, n, nrhs) * sizeof(double2) + 256;
+  const size_t df = (((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255)) +
+                    residual_partial_elems(n, n, nrhs) * sizeof(double2) + 256;
+  *bytes = std::max(df, residual_tc_workspace_bytes(n, n, nrhs));
   return MGT_OK;
 }
 
@@ -322,7 +358,12 @@ extern "C" int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X
                             void* stream) {
   if (!M || !X || !B || !R || !work || n <= 0 || nrhs <= 0 || ldm < n || ldx < nrhs || ldb < nrhs || ldr < nrhs)
     return MGT_ERR_ARG;
-  if (n > (1 << 30) || work_bytes < (size_t)n * nrhs * sizeof(float4)) return MGT_ERR_WORKSPACE;
+  if (n > (1 << 30)) return MGT_ERR_WORKSPACE;
+  // tensor cores when the workspace holds their buffers
+  if (residual_tc_supported(n, n, nrhs) && work_bytes >= residual_tc_workspace_bytes(n, n, nrhs))
+    return residual_tc((const float4*)M, ldm, (int)n, (int)n, (const double2*)X, ldx, (int)nrhs, (const double2*)B,
+                       ldb, (double2*)R, ldr, nullptr, work, work_bytes, (cudaStream_t)stream);
+  if (work_bytes < (size_t)n * nrhs * sizeof(float4)) return MGT_ERR_WORKSPACE;
   // split-K partials after the double-float copy of X, as far as the workspace holds them
   const size_t xs_bytes = ((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255);
   double2* part = nullptr;
@@ -370,24 +411,29 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 1);
   double prev = 0.0, rel = 0.0;
   int it = 0;
+  int dev_status = MGT_OK;
   for (;; ++it) {
-    e = residual_impl((const float4*)M, ldm, Xd, ldx, Bd, ldb, w.Rr, nr, nn, nr, w.Xs, w.part, w.part_elems, s);
+    e = w.residual((const float4*)M, ldm, Xd, ldx, Bd, ldb, nn, nr, it > 0, s);
     if (e != MGT_OK) return e;
     if (cudaMemsetAsync(w.norms + 1, 0, sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
     count_launch();
-  sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, w.norms + 1);
+    sumsq_kernel<<<std::min<int64_t>(1024, (tot + 255) / 256), 256, 0, s>>>(w.Rr, nr, nn, nr, w.norms + 1);
     if (cudaMemcpyAsync(h, w.norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MGT_ERR_CUDA;
+    if (w.status() &&
+        cudaMemcpyAsync(&dev_status, w.status(), sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return MGT_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return MGT_ERR_CUDA;
+    if (dev_status != MGT_OK) return dev_status;
     rel = h[0] > 0 ? sqrt(h[1] / h[0]) : sqrt(h[1]);
     if (rel <= tol || it >= max_iter) break;
     if (it > 0 && !(rel < 0.9 * prev)) break;  // stagnation or divergence
     prev = rel;
     count_launch();
-  c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
+    c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
     e = mgt_lu_solve(MGT_C64, LU, n, ldlu, perm, w.R32, nr, w.D32, nr, nrhs, w.tri, tri_bytes, stream);
     if (e != MGT_OK) return e;
     count_launch();
-  c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
+    c64_into_c128_kernel<<<eg, 256, 0, s>>>(w.D32, nr, Xd, ldx, nn, nr, 0);
   }
   if (iters) *iters = it;
   if (rel_res) *rel_res = rel;
@@ -460,8 +506,7 @@ extern "C" int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, in
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const unsigned eg = (unsigned)((n * nrhs + 255) / 256);
-  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs,
-                        w.part, w.part_elems, s);
+  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, false, s);
   if (e != MGT_OK) return e;
   count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
@@ -483,8 +528,7 @@ extern "C" int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const voi
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const int64_t tot = n * nrhs;
-  int e = residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, w.Rr, nr, nn, nr, w.Xs,
-                        w.part, w.part_elems, s);
+  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, false, s);
   if (e != MGT_OK) return e;
   if (cudaMemsetAsync(norms_dev, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
   count_launch(2);

@@ -11,8 +11,12 @@ complex128 LU with partial pivoting, complex128 triangular solves.
 
 ``"mixed"``: one assembly pass writes the matrix in complex64 (for the LU) and
 in double-float form (for residuals); the LU runs in complex64 and iterative
-refinement with double-float residuals brings the solution to a relative
-residual ``tol`` (1e-10 by default), i.e. complex128-level accuracy.
+refinement brings the solution to a relative residual ``tol`` (1e-10 by
+default), i.e. complex128-level accuracy.  The residuals run on the tensor
+cores (a digit-split product of the double-float matrix).  The LU chooses its
+pivots within each 64-row diagonal tile (no exchange between CTAs); when the
+refinement cannot use such factors (or a tile pivot is exactly zero) the
+matrix is factored again with partial pivoting.
 """
 from __future__ import annotations
 
@@ -127,16 +131,25 @@ def assemble_propagator(kind, targets, sources, k0, coef=1.0, regularize=False, 
 class LUFactors:
     """In-place LU factors with their row permutation and workspace."""
 
-    def __init__(self, lu, perm, work, dtype_code):
+    def __init__(self, lu, perm, work, dtype_code, pivoting="partial"):
         self.lu, self.perm, self.work, self.dtype_code = lu, perm, work, dtype_code
+        self.pivoting = pivoting
 
     @property
     def n(self):
         return self.lu.shape[0]
 
 
-def lu_factor(A, check_singular=True):
-    """Factor A (complex128 or complex64, n x n, CUDA) in place."""
+PIVOTING = {"partial": L.MGT_PIVOT_PARTIAL, "tile": L.MGT_PIVOT_TILE}
+
+
+def lu_factor(A, check_singular=True, pivoting="partial", options=None):
+    """Factor A (complex128 or complex64, n x n, CUDA) in place.
+
+    pivoting: "partial" (LAPACK's row interchanges, the reference's pivot
+    sequence) or "tile" (complex64: pivots chosen within each 64-row
+    diagonal tile, no exchange between CTAs; for the refined mixed method).
+    options: an _lib.LuOptions for the other per-call choices."""
     lib = L.load()
     _need_cuda(A, "A")
     n = A.shape[0]
@@ -145,12 +158,22 @@ def lu_factor(A, check_singular=True):
     L.check(lib.mgt_lu_workspace_bytes(code, n, ctypes.byref(nb)), "mgt_lu_workspace_bytes")
     work = workspace(nb.value, A.device)
     perm = torch.empty(n, dtype=torch.int32, device=A.device)
-    L.check(lib.mgt_lu_factor(code, _ptr(A), n, A.stride(0), _ptr(perm), _ptr(work), work.numel(), _stream()),
-            "mgt_lu_factor")
-    f = LUFactors(A, perm, work, code)
+    opt = options if options is not None else L.LuOptions()
+    opt.pivoting = PIVOTING[pivoting] if options is None else opt.pivoting
+    L.check(lib.mgt_lu_factor_ex(code, _ptr(A), n, A.stride(0), _ptr(perm), _ptr(work), work.numel(),
+                                 ctypes.byref(opt), _stream()), "mgt_lu_factor_ex")
+    f = LUFactors(A, perm, work, code, "tile" if opt.pivoting == L.MGT_PIVOT_TILE else "partial")
     if check_singular:
         status_check(f)
     return f
+
+
+def lu_info(f):
+    """(device error, first zero pivot) of a factorisation; synchronises the stream."""
+    lib = L.load()
+    st = (ctypes.c_int32 * 2)()
+    L.check(lib.mgt_workspace_status(_ptr(f.work), st, _stream()), "mgt_workspace_status")
+    return st[0], st[1]
 
 
 def status_check(f):
@@ -228,12 +251,41 @@ def solve_system(kind, points, k0, coef, shift, E0, precision="fp64", tol=DEFAUL
         return X
     if precision == "mixed":
         Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
-        f = lu_factor(M32)
-        X, it, rr = solve_refined(Mdf, f, E0, tol, max_iter)
+        f, X, it, rr = mixed_factor_solve(Mdf, M32, E0, _fresh(kind, points, k0, coef, shift), tol, max_iter)
         if stats is not None:
-            stats.update(method="mixed", iterations=it, rel_residual=rr)
+            stats.update(method="mixed", iterations=it, rel_residual=rr, pivoting=f.pivoting)
         return X
     raise ValueError(f"unknown precision {precision!r} (expected 'fp64' or 'mixed')")
+
+
+def mixed_factor(M32, fresh_m32):
+    """complex64 LU of M32 with tile pivoting; with partial pivoting of a fresh
+    copy (fresh_m32() returns one) when a tile pivot is exactly zero."""
+    f = lu_factor(M32, check_singular=False, pivoting="tile")
+    err, info = lu_info(f)
+    if err != 0:
+        raise L.MagreeteError(err, "mgt_lu_factor_ex (device)")
+    if info == 0:
+        return f
+    return lu_factor(fresh_m32(), pivoting="partial")
+
+
+def mixed_factor_solve(Mdf, M32, B, fresh_m32, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER):
+    """Factor M32 (tile pivoting first) and refine M X = B against the
+    double-float Mdf; if the refinement does not reach tol on tile-pivoted
+    factors, factor a fresh copy with partial pivoting and refine again.
+    Returns (factors, X, iterations, relative residual)."""
+    f = mixed_factor(M32, fresh_m32)
+    X, it, rr = solve_refined(Mdf, f, B, tol, max_iter, require=f.pivoting == "partial")
+    if rr <= tol:
+        return f, X, it, rr
+    f = lu_factor(fresh_m32(), pivoting="partial")
+    X, it, rr = solve_refined(Mdf, f, B, tol, max_iter)
+    return f, X, it, rr
+
+
+def _fresh(kind, points, k0, coef, shift):
+    return lambda: assemble_system(kind, points, k0, coef, shift, ("c64",))[0]
 
 
 class SystemFactorization:
@@ -249,7 +301,8 @@ class SystemFactorization:
             self.f = lu_factor(M)
         elif precision == "mixed":
             self.Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
-            self.f = lu_factor(M32)
+            self._fresh = _fresh(kind, points, k0, coef, shift)
+            self.f = mixed_factor(M32, self._fresh)
         else:
             raise ValueError(f"unknown precision {precision!r}")
         self.last_iterations = 0
@@ -258,7 +311,12 @@ class SystemFactorization:
     def solve(self, B):
         if self.precision == "fp64":
             return lu_solve(self.f, B.to(torch.complex128))
-        X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter)
+        B = B.to(torch.complex128)
+        X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter, require=self.f.pivoting == "partial")
+        if rr > self.tol:
+            # tile-pivoted factors that refinement cannot use: partial pivoting from here on
+            self.f = lu_factor(self._fresh(), pivoting="partial")
+            X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter)
         self.last_iterations, self.last_residual = it, rr
         return X
 

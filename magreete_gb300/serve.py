@@ -78,14 +78,16 @@ def matrix_bytes(prob, precision="mixed"):
     mixed: complex64 LU + double-float residual copy; 16 B fp64), the
     tensor-core split buffers (3 KB per row), the right-hand-side blocks and
     the propagation workspace (double-float propagator rows, at most 1 GiB at
-    a time, and the double-float copy of the fields) and the split-K partial
-    sums of the residual (at most 16 splits of 64 columns)."""
+    a time, and the double-float copy of the fields), the split-K partial sums
+    of the residual (at most 16 splits) and the digit blocks of the
+    tensor-core residual (56 KB per 32 rows and 32 right-hand sides)."""
     n, R = prob.n, prob.nrhs
     per = 16 if precision == "fp64" else 24
     T = prob.detectors.shape[0] if prob.detectors is not None else 0
     prop = min(1 << 30, 16 * prob.d * n * T) + 16 * n * R
-    partial = 16 * 16 * n * min(R, 64)
-    return per * n * n + 3072 * n + 8 * 16 * n * R + prop + partial + (64 << 20)
+    partial = 16 * 16 * n * max(R, 64)
+    digits = 57344 * -(-n // 32) * -(-R // 32)
+    return per * n * n + 3072 * n + 8 * 16 * n * R + prop + partial + digits + (64 << 20)
 
 
 def serve_sequential(problems, precision="mixed", device_inputs=None, start=None):
