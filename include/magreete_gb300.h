@@ -198,12 +198,15 @@ int mgt_workspace_status(void* work, int32_t out[2], void* stream);
 
 /*
  * Residual R = B - M X with M (n x n) in MGT_CDF form, X, B, R complex128
- * (n x nrhs), computed in double-float arithmetic on the FP32 pipes
- * (products exact via fma, sums compensated).  `work` must hold at least
- * n * nrhs * 16 bytes (the double-float copy of X); the
- * mgt_residual_workspace_bytes(n, nrhs) size adds room for split-K partial
- * sums, and whatever the workspace holds beyond the copy of X is used for
- * them (more CTAs over K: fewer idle SMs).  Used by iterative refinement.
+ * (n x nrhs).  With a workspace of mgt_residual_workspace_bytes(n, nrhs)
+ * bytes it runs on the tensor cores: M and X are split into seven 8-bit
+ * digits per entry (row / column power-of-two scales), digit pairs of equal
+ * weight accumulate exactly in FP32 on tcgen05 and exactly in 64-bit
+ * integers across K (error ~1e-14 of ||B|| on system matrices; within
+ * n 2^-48 of |M||X| entry-wise).  A workspace of exactly n * nrhs * 16
+ * bytes (the double-float copy of X) selects double-float arithmetic on the
+ * FP32 pipes (products exact via fma, sums compensated), unsplit.  Used by
+ * iterative refinement.
  */
 int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
 int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X, int64_t ldx,
@@ -243,10 +246,14 @@ int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const void* B, int64
                      int64_t nrhs, void* work, size_t work_bytes, double* norms_dev, void* stream);
 
 /*
- * Matrix-free propagation to detectors:
+ * Propagation to detectors:
  *   out[m*d + a, r] = coef * sum_{j,b} G_ab(t_m - s_j) Ek[j*d + b, r] + E0[m*d + a, r]
- * G is recomputed on the fly in FP64 and never stored; the contraction runs
- * in FP64 (dtype MGT_C128) or double-float on the FP32 pipes (MGT_CDF).
+ * dtype MGT_C128 (the plain method): matrix-free, G is recomputed on the fly
+ * in FP64 and contracted in FP64, never stored.  MGT_CDF (the mixed method):
+ * the rows -coef G are evaluated in FP64, stored double-float in chunks of at
+ * most 1 GiB of the workspace and contracted with Ek by the tensor-core
+ * residual kernel (out = E0 - (-coef G) Ek; see mgt_residual), or in
+ * double-float on the FP32 pipes where the tensor cores are unavailable.
  * Ek, E0 and out are complex128 in both cases.  Replaces the dense
  * G0(points) + matmul of propagate() (Transmission2D.py:190, :701;
  * Transmission3D.py:163, :675) and propagate_ss().  Rows where the

@@ -22,6 +22,7 @@
 #include "df.cuh"
 #include "green.cuh"
 #include "diag.cuh"
+#include "residual_tc.cuh"
 
 namespace mgt {
 
@@ -223,6 +224,15 @@ static size_t prop_part_elems(int64_t nt, int64_t ns, int64_t nrhs, int d) {
 static size_t prop_df_bytes(int64_t nt, int64_t ns, int64_t nrhs, int d) {
   return prop_xs_bytes(ns, nrhs, d) + prop_chunk_bytes(nt, ns, d) + prop_part_elems(nt, ns, nrhs, d) * sizeof(double2);
 }
+// tensor-core contraction: one chunk of propagator rows | the residual kernel's workspace
+static bool prop_tc_ok(int64_t nt, int64_t ns, int64_t nrhs, int d) {
+  return residual_tc_supported(prop_chunk_targets(nt, ns, d) * d, (int64_t)d * ns, nrhs);
+}
+static size_t prop_tc_bytes(int64_t nt, int64_t ns, int64_t nrhs, int d) {
+  if (!prop_tc_ok(nt, ns, nrhs, d)) return 0;
+  return prop_chunk_bytes(nt, ns, d) +
+         residual_tc_workspace_bytes(prop_chunk_targets(nt, ns, d) * d, (int64_t)d * ns, nrhs) + 1024;
+}
 
 static int kind_dim_d(int kind, int* dim) {
   switch (kind) {
@@ -246,8 +256,8 @@ extern "C" int mgt_propagate_workspace_bytes(int kind, int64_t n_targets, int64_
   int nsplit = choose_splits(n_targets, n_sources);
   // the larger of the two methods' needs: FP64 partial sums, or the
   // double-float copy of Ek plus one chunk of assembled propagator rows
-  *bytes = std::max((size_t)nsplit * n_targets * d * std::min<int64_t>(nrhs, kPCols) * sizeof(double2),
-                    prop_df_bytes(n_targets, n_sources, nrhs, d));
+  *bytes = std::max({(size_t)nsplit * n_targets * d * std::min<int64_t>(nrhs, kPCols) * sizeof(double2),
+                     prop_df_bytes(n_targets, n_sources, nrhs, d), prop_tc_bytes(n_targets, n_sources, nrhs, d)});
   return MGT_OK;
 }
 
@@ -267,6 +277,28 @@ extern "C" int mgt_propagate(int kind, int dtype, const double* targets, int64_t
   if (work_bytes < need) return MGT_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   const int nt = (int)n_targets, ns = (int)n_sources;
+  if (dtype == MGT_CDF && prop_tc_ok(nt, ns, nrhs, d)) {
+    // propagator rows (-coef G, double-float) contracted on the tensor cores:
+    // out = E0 - (-coef G) Ek; rows with NaN blocks (a detector on a scatterer)
+    // come out NaN for the host's fix-up
+    const int64_t ct = prop_chunk_targets(nt, ns, d);
+    float4* Gc = (float4*)work;
+    char* tw = (char*)work + ((prop_chunk_bytes(nt, ns, d) + 1023) & ~size_t(1023));
+    const size_t tw_bytes = work_bytes - (size_t)(tw - (char*)work);
+    const double2 mcoef = make_double2(-coef_re, -coef_im);
+    const double2 nanfill = make_double2(0.0, 0.0);
+    int e = MGT_OK;
+    for (int64_t t0 = 0; t0 < nt && e == MGT_OK; t0 += ct) {
+      const int tc = (int)std::min<int64_t>(ct, nt - t0);
+      e = assemble_propagator_into(kind, targets + t0 * dim, tc, sources, ns, k0, mcoef, regularize != 0, radius,
+                                   MGT_NAN_KEEP, nanfill, 0, Gc, (int64_t)d * ns, MGT_CDF, st);
+      if (e != MGT_OK) break;
+      const double2* b = E0 ? (const double2*)E0 + t0 * d * ld_e0 : nullptr;
+      e = residual_tc(Gc, (int64_t)d * ns, tc * d, d * ns, (const double2*)Ek, ld_ek, (int)nrhs, b, ld_e0,
+                      (double2*)out + t0 * d * ld_out, ld_out, nullptr, tw, tw_bytes, st);
+    }
+    return e;
+  }
   if (dtype == MGT_CDF) {
     const int64_t ct = prop_chunk_targets(nt, ns, d);
     float4* Xs = (float4*)work;

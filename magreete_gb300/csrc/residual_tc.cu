@@ -108,6 +108,9 @@ __device__ __forceinline__ float digit_f(long long y, int p) {
   return __int_as_float(0x4B400000 | (int)byte) - 12583040.0f;   // byte - 128
 }
 
+// row exponent of a row holding a NaN or an infinity: its outputs are NaN
+constexpr int kRowNonFinite = 0x40000000;
+
 __device__ __forceinline__ int clamp_exp(int e) { return (e < -300 || e > 300) ? 0 : e; }
 
 // Byte offset of real K index kr (even) of row rho in a 128-row tile whose rows
@@ -249,7 +252,7 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
     }
     const int row = row0 + r;
     if (row < rows) {
-      const bool good = ok && !*abort;
+      const bool good = ok && !*abort && row_exp[row] != kRowNonFinite;
       const int ea = rexp[r];
       for (int jc = 0; jc < BNC; ++jc) {
         const int col = ct * BNC + jc;
@@ -313,7 +316,8 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
   }
 }
 
-// e_i of each row: 2^e_i bounds the row's largest |re|, |im| (hi parts); one warp per row
+// e_i of each row: 2^e_i bounds the row's largest |re|, |im| (hi parts); one
+// warp per row.  Rows with a NaN or an infinity get kRowNonFinite.
 __global__ void rowexp_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim, int* __restrict__ out) {
   const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (row >= rows) return;
@@ -324,7 +328,8 @@ __global__ void rowexp_kernel(const float4* __restrict__ M, int64_t ldm, int row
   }
   m = __reduce_max_sync(0xffffffffu, m);
   int e = 0;
-  if (m != 0u) frexpf(__uint_as_float(m), &e);
+  if (m >= 0x7F800000u) e = kRowNonFinite;
+  else if (m != 0u) frexpf(__uint_as_float(m), &e);
   if (lane == 0) out[row] = e;
 }
 

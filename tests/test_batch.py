@@ -38,13 +38,31 @@ def test_graph_replay_matches_eager():
 
 
 def test_autotune_picks_and_caches(tmp_path):
+    """The autotuner times every candidate, caches the fastest per size
+    bucket, and leaves the library's process-wide tuning as it was."""
     from magreete_gb300 import batch, _lib
+    lib = _lib.load()
+    before = [lib.mgt_get_tuning(k) for k in range(1, 11)]
     probs = sweep_problems(4, seed=5)
     cache = str(tmp_path / "tune.json")
-    best = batch.autotune(probs, branch_options=(2, 4), panel_rows_options=(128, 256), cache=cache)
-    assert best["branches"] in (2, 4) and best["panel_rows"] in (128, 256)
+    best = batch.autotune(probs, branch_options=(2, 4), pivoting_options=("tile", "partial"), outer_options=(128,),
+                          cache=cache)
+    assert best["branches"] in (2, 4) and best["pivoting"] in ("tile", "partial") and best["outer_block"] == 128
     assert len(best["candidates"]) == 4
     again = batch.autotune(probs, cache=cache)     # served from the cache
-    assert again["branches"] == best["branches"]
-    assert _lib.load().mgt_get_tuning(_lib.MGT_TUNE_PANEL_ROWS) == best["panel_rows"]
-    _lib.load().mgt_set_tuning(_lib.MGT_TUNE_PANEL_ROWS, 256)
+    assert {k: again[k] for k in ("branches", "pivoting", "outer_block")} == \
+        {k: best[k] for k in ("branches", "pivoting", "outer_block")}
+    assert [lib.mgt_get_tuning(k) for k in range(1, 11)] == before
+
+
+def test_partial_pivoting_graph_matches_eager():
+    """Graph replays of partially pivoted (LAPACK-order) factorisations."""
+    from magreete_gb300 import batch, serve
+    probs = sweep_problems(4, seed=9)
+    sw = batch.BatchedSweep(probs, branches=2, pivoting="partial")
+    sw.warmup()
+    sw.capture()
+    extra, res = sw.replay()
+    assert max(res) <= 1e-10
+    for p, X in zip(probs, sw.solutions()):
+        assert rel(X, serve.solve_problem(p, "mixed").Ek) < 1e-8
