@@ -386,6 +386,78 @@ def vs_plain_fp64(srv, wins, dev_inputs):
             "max_field_err_vs_fp64": {"Ek": max(ek), "E_det": max(ed)}}
 
 
+def secondary_rooflines():
+    """The two other kernels with large shares of the stream, timed alone with
+    CUDA events after the timed region:
+      * the tensor-core refinement residual R = B - M X (3D N=4000: n = 12000,
+        64 right-hand sides).  Its algorithmic work is the 28 digit-pair real
+        products of the FP16 digit split, 224 n^2 R tensor flops (8 n^2 R per
+        product), held to the measured bf16 (= fp16) dense peak;
+      * the complex64 LU of order 2000 (2D N=1000), where the trailing update is
+        small and the time is the panel chain's latency, tile and partial
+        pivoting."""
+    from magreete_gb300 import engine as E, selfterm
+    from magreete_gb300 import workloads as W
+    hbm, bf16, src = measured_peaks()
+    dev = torch.device("cuda")
+    out = {}
+    prob = W.cfg2()
+    pts = prob.points.to(dev)
+    coef = prob.alpha * prob.k0 ** 2
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    (Mdf,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf",))
+    n, R = prob.n, prob.nrhs
+    gen = torch.Generator(device=dev).manual_seed(5)
+    X = torch.randn(n, R, dtype=torch.complex128, device=dev, generator=gen)
+    B = torch.randn(n, R, dtype=torch.complex128, device=dev, generator=gen)
+    for _ in range(2):
+        E.residual(Mdf, X, B)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        E.residual(Mdf, X, B)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    tflop = 224.0 * n * n * R / 1e12
+    nbytes = 16.0 * n * n + 3 * 16.0 * n * R
+    out["residual_tc"] = {"kernel": "rtc::residual_tc_kernel (+ row / column scales, right-hand-side digits, "
+                                    "reduction of the K splits)",
+                          "bound": "tensor", "n": n, "nrhs": R, "ms": ms,
+                          "achieved": tflop / (ms * 1e-3), "peak": bf16, "unit": "TFLOP/s",
+                          "frac": tflop / (ms * 1e-3) / bf16,
+                          "algorithmic_tflop": tflop,
+                          "hbm_achieved_gbs": nbytes / (ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm,
+                          "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / hbm,
+                          "peak_source": f"bf16_tflops of {src} peaks (kind::f16 runs at the bf16 rate); "
+                                         "224 n^2 R flops = 28 digit-pair products of the 7-digit split",
+                          "complex_macs_per_s": float(n) * n * R / (ms * 1e-3)}
+    del Mdf, X, B
+    prob = W.cfg1()
+    pts = prob.points.to(dev)
+    coef = prob.alpha * prob.k0 ** 2
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    (M32,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("c64",))
+    for piv in ("tile", "partial"):
+        ts = []
+        for rep in range(4):
+            A = torch.empty_strided(M32.size(), M32.stride(), dtype=M32.dtype, device=dev)
+            A.copy_(M32)
+            torch.cuda.synchronize()
+            e0.record()
+            E.lu_factor(A, check_singular=False, pivoting=piv)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        lu_ms = min(ts[1:])
+        out[f"lu_panel_{piv}"] = {"bound": "latency (the panel chain)", "n": prob.n, "pivoting": piv,
+                                  "lu_ms": lu_ms, "us_per_column": 1e3 * lu_ms / prob.n,
+                                  "note": "complex64 LU of order 2000; the trailing update is a small part of it"}
+    return out
+
+
 def sweep_measure(count, group):
     """The batched 2D sweep (TE disk, N uniform in [500, 4000], 16 angles):
     groups of instances captured into one CUDA graph each, concurrency,

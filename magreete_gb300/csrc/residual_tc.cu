@@ -13,17 +13,20 @@
 //    row i = Mr_i0, Mi_i0, Mr_i1, Mi_i1, ...) and B'^T (2 nrhs x 2 kdim: row
 //    2j = Xr_0j, -Xi_0j, ...; row 2j+1 = Xi_0j, Xr_0j, ...).
 //  * Row i of A' is scaled by 2^-e_i, 2^e_i bounding the row's largest
-//    |re|, |im|, and every entry becomes the 56-bit integer
-//    round((hi + lo) 2^(55 - e_i)) = sum_{p=0..6} d_p 256^p with balanced
-//    digits: d_0 .. d_5 in [-128, 127], d_6 in [-128, 128].  The columns of
-//    B' are scaled by their own power of two the same way.
+//    |re|, |im|, and every entry becomes the integer
+//    X = round((hi + lo) 2^(54 - e_i)), |X| < 2^54, written with seven
+//    balanced base-256 digits X = sum_{p=0..6} d_p 256^p: the bytes of
+//    X + 128 (256^0 + ... + 256^6) minus 128, so d_0 .. d_5 lie in
+//    [-128, 127] and the top digit d_6 in [-64, 64].  The columns of B' are
+//    scaled by their own power of two the same way.
 //  * A digit needs at most 8 bits and is exact in FP16; a product of two is
 //    at most 2^14.  Counting digits from the top (s = 6 - p), the pairs
 //    (s, t) with s + t = l share the weight 256^-l and accumulate in one
 //    TMEM accumulator per level l = 0 .. 6; pairs with s + t > 6 lie below
-//    2^-56 of the row and column scales and are not formed.  A level
-//    receives at most 7 pairs x 128 products (7 * 2^21 < 2^24) before it is
-//    read out, so its FP32 sum is an exact integer.
+//    2^-55 of the row and column scales and are not formed.  A level
+//    receives at most 7 pairs x 128 products (6 * 2^21 < 2^24 with the
+//    smaller top digits) before it is read out, so its FP32 sum is an exact
+//    integer.
 //  * Every 128 real K the level sums are read out of TMEM and folded into
 //    one 64-bit integer per output in units of 2^-48 of the row and column
 //    scales: levels 0 .. 4 exactly, 5 and 6 rounded to the nearest unit.  A
@@ -45,9 +48,12 @@
 //                10 MMAs per K step instead of 28, A read once per MMA)
 //   warp 2     : TMEM allocation (7 levels x 64 columns)
 //   warps 4-7  : epilogue, thread = row: level sums -> 64-bit accumulators
-//   warps 8-15 : converters: double-float entries of M -> digits, written
-//                straight into the 128-byte-swizzled K-major layout of the
-//                MMA's A operand, one digit slice at a time through a ring
+//   warps 8-23 : converters, eight rows each: the double-float entries of M
+//                are loaded for a whole chunk at once, turned into 54-bit
+//                integers, and their digits (one byte permute, one logic op
+//                and one fp16 subtract per re / im pair) written straight
+//                into the 128-byte-swizzled K-major layout of the MMA's A
+//                operand, one digit slice at a time through a ring
 // Every wait is bounded; a CTA whose wait runs out writes NaN outputs, sets
 // MGT_ERR_TIMEOUT in the status word, drains what it issued and returns.
 #include <cuda_fp16.h>
@@ -74,17 +80,18 @@ constexpr uint32_t B_SLICE = BN * 128;              // 8 KB
 constexpr uint32_t B_BLOCK = DIG * B_SLICE;         // 56 KB: one chunk of B', all digit slices
 constexpr uint32_t W_BYTES = BM * BN * 8;           // 64-bit accumulators
 constexpr uint32_t TMEM_COLS = 512;
-constexpr int NCONV = 8, NEPI = 4;
+constexpr int NCONV = 16, NEPI = 4;
 constexpr int THREADS = (4 + NEPI + NCONV) * 32;
-constexpr int ROWS_PER_CONV = BM / NCONV;           // 16
+constexpr int ROWS_PER_CONV = BM / NCONV;           // 8
 // at most 512 chunks (32768 real K) per CTA: |sum| <= 2^15 * 2^48 = 2^63
 // units of 2^-48, less the rounding of levels 5 and 6
 constexpr int MAX_SPLIT_CHUNKS = 512;
-constexpr long long BIAS = 0x0000808080808080LL;    // 128 in each of the six lower digit positions
+constexpr long long BIAS = 0x0080808080808080LL;    // 128 in each of the seven digit positions
+constexpr int FIX = 54;                             // |X| < 2^FIX
 
 constexpr size_t smem_bytes() { return 1024 + ASLOTS * A_SLICE + 2 * B_BLOCK + W_BYTES + BM * sizeof(int) + 256; }
 
-// round(f * 2^sh) as a 64-bit integer (|f| * 2^sh < 2^56 by the row scale);
+// round(f * 2^sh) as a 64-bit integer (|f| * 2^sh < 2^54 by the row scale);
 // zero and subnormal f (below 2^-126) give 0
 __device__ __forceinline__ long long fixed_point(float f, int sh) {
   const uint32_t u = __float_as_uint(f);
@@ -99,14 +106,40 @@ __device__ __forceinline__ long long fixed_point(float f, int sh) {
   return (u >> 31) ? -r : r;
 }
 
+// round(f * 2^sh) for the low part of a double-float entry (|f| * 2^sh < 2^30):
+// one exact power-of-two multiply and one conversion
+__device__ __forceinline__ long long fixed_low(float f, int sh) {
+  if (sh > 127 || sh < -126) return fixed_point(f, sh);
+  return (long long)__float2int_rn(f * __int_as_float((127 + sh) << 23));
+}
+
 // Digit at position p (0 = lowest) of y = X + BIAS, as an exact float.
 __device__ __forceinline__ float digit_f(long long y, int p) {
   const uint32_t lo = (uint32_t)y, hi = (uint32_t)((unsigned long long)y >> 32);
-  if (p == DIG - 1) return __int_as_float(0x4B400000 + ((int)hi >> 16)) - 12582912.0f;
   const uint32_t w = p < 4 ? lo : hi;
   const uint32_t byte = (w >> (8 * (p & 3))) & 255u;
   return __int_as_float(0x4B400000 | (int)byte) - 12583040.0f;   // byte - 128
 }
+
+// fp16 pair (digit P of yr, digit P of yi) as one 32-bit word: the two bytes
+// are picked by one byte permute, turned into the fp16 encodings of
+// 1024 + byte, and 1152 is subtracted (byte - 128, exact)
+template <int P>
+__device__ __forceinline__ uint32_t digit_pair(long long yr, long long yi) {
+  const uint32_t wr = P < 4 ? (uint32_t)yr : (uint32_t)((unsigned long long)yr >> 32);
+  const uint32_t wi = P < 4 ? (uint32_t)yi : (uint32_t)((unsigned long long)yi >> 32);
+  constexpr uint32_t b = P & 3;
+  const uint32_t x = __byte_perm(wr, wi, b | (b << 4) | ((4 + b) << 8) | ((4 + b) << 12));
+  const uint32_t h = (x & 0x00FF00FFu) | 0x64006400u;
+  const __half2 c = __halves2half2(__ushort_as_half((unsigned short)0x6480), __ushort_as_half((unsigned short)0x6480));
+  const __half2 d = __hsub2(*reinterpret_cast<const __half2*>(&h), c);
+  return *reinterpret_cast<const uint32_t*>(&d);
+}
+
+// one digit slice of a converter warp's rows: row cw + NCONV t, lane = complex column
+template <int P>
+__device__ __forceinline__ void conv_pass(unsigned char* tile, const long long (&yr)[ROWS_PER_CONV],
+                                          const long long (&yi)[ROWS_PER_CONV], int cw, int lane);
 
 // row exponent of a row holding a NaN or an infinity: its outputs are NaN
 constexpr int kRowNonFinite = 0x40000000;
@@ -118,6 +151,14 @@ __device__ __forceinline__ int clamp_exp(int e) { return (e < -300 || e > 300) ?
 // XOR-swizzled by the row within its group: the K-major 128B-swizzle layout.
 __device__ __forceinline__ uint32_t swz(int rho, int kr) {
   return (uint32_t)rho * 128u + ((uint32_t)(((kr >> 3) ^ (rho & 7)) << 4)) + (uint32_t)((kr & 7) * 2);
+}
+
+template <int P>
+__device__ __forceinline__ void conv_pass(unsigned char* tile, const long long (&yr)[ROWS_PER_CONV],
+                                          const long long (&yi)[ROWS_PER_CONV], int cw, int lane) {
+#pragma unroll
+  for (int t = 0; t < ROWS_PER_CONV; ++t)
+    *reinterpret_cast<uint32_t*>(tile + swz(cw + NCONV * t, 2 * lane)) = digit_pair<P>(yr[t], yi[t]);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -238,14 +279,14 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          // level l weighs 2^(34 - 8 l) units of 2^-48
+          // level l weighs 2^(36 - 8 l) units of 2^-48
           const long long low = ((long long)__float2int_rz(__uint_as_float(v[5][j])) << 8) +
                                 (long long)__float2int_rz(__uint_as_float(v[6][j]));
-          const long long w = ((long long)__float2int_rz(__uint_as_float(v[0][j])) << 34) +
-                              ((long long)__float2int_rz(__uint_as_float(v[1][j])) << 26) +
-                              ((long long)__float2int_rz(__uint_as_float(v[2][j])) << 18) +
-                              ((long long)__float2int_rz(__uint_as_float(v[3][j])) << 10) +
-                              ((long long)__float2int_rz(__uint_as_float(v[4][j])) << 2) + ((low + 8192) >> 14);
+          const long long w = ((long long)__float2int_rz(__uint_as_float(v[0][j])) << 36) +
+                              ((long long)__float2int_rz(__uint_as_float(v[1][j])) << 28) +
+                              ((long long)__float2int_rz(__uint_as_float(v[2][j])) << 20) +
+                              ((long long)__float2int_rz(__uint_as_float(v[3][j])) << 12) +
+                              ((long long)__float2int_rz(__uint_as_float(v[4][j])) << 4) + ((low + 2048) >> 12);
           wacc[(p * 8 + j) * BM + r] += w;
         }
       }
@@ -273,35 +314,55 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
       }
     }
   } else if (warp >= 4 + NEPI) {
-    // ---------------- converters: rows cw, cw + 8, ...; lane = complex column of the chunk
+    // ---------------- converters: rows cw, cw + NCONV, ...; lane = complex column of the chunk
     const int cw = warp - 4 - NEPI;
     int q = 0;
-    for (int i = 0; i < nchunk && !*abort; ++i) {
+    float4 v[ROWS_PER_CONV];
+    auto load_chunk = [&](int i) {
       const int kc = (c_begin + i) * KCC + lane;
+#pragma unroll
+      for (int t = 0; t < ROWS_PER_CONV; ++t) {
+        const int row = row0 + cw + NCONV * t;
+        v[t] = (i < nchunk && row < rows && kc < kdim) ? __ldg(&M[(int64_t)row * ldm + kc])
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    };
+    load_chunk(0);
+    for (int i = 0; i < nchunk && !*abort; ++i) {
       long long yr[ROWS_PER_CONV], yi[ROWS_PER_CONV];
 #pragma unroll
       for (int t = 0; t < ROWS_PER_CONV; ++t) {
-        const int rl = cw + NCONV * t, row = row0 + rl;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (row < rows && kc < kdim) v = __ldg(&M[(int64_t)row * ldm + kc]);
-        const int sh = 55 - rexp[rl];
-        yr[t] = fixed_point(v.x, sh) + fixed_point(v.y, sh) + BIAS;
-        yi[t] = fixed_point(v.z, sh) + fixed_point(v.w, sh) + BIAS;
+        const int sh = FIX - rexp[cw + NCONV * t];
+        yr[t] = fixed_point(v[t].x, sh) + fixed_low(v[t].y, sh) + BIAS;
+        yi[t] = fixed_point(v[t].z, sh) + fixed_low(v[t].w, sh) + BIAS;
       }
-      for (int s = 0; s < DIG; ++s, ++q) {
-        const int slot = q % ASLOTS;
-        if (q >= ASLOTS && !mbar_wait(&empty_a[slot], ((q / ASLOTS) - 1) & 1, abort)) break;
-        unsigned char* tile = aring + slot * A_SLICE;
-        const int p = DIG - 1 - s;
+      bool ok = true;
 #pragma unroll
-        for (int t = 0; t < ROWS_PER_CONV; ++t) {
-          const int rl = cw + NCONV * t;
-          *reinterpret_cast<__half2*>(tile + swz(rl, 2 * lane)) = __floats2half2_rn(digit_f(yr[t], p), digit_f(yi[t], p));
+      for (int s = 0; s < DIG; ++s) {
+        const int slot = (q + s) % ASLOTS;
+        if (ok && q + s >= ASLOTS && !mbar_wait(&empty_a[slot], (((q + s) / ASLOTS) - 1) & 1, abort)) ok = false;
+        if (ok) {
+          unsigned char* tile = aring + slot * A_SLICE;
+          switch (DIG - 1 - s) {
+            case 0: conv_pass<0>(tile, yr, yi, cw, lane); break;
+            case 1: conv_pass<1>(tile, yr, yi, cw, lane); break;
+            case 2: conv_pass<2>(tile, yr, yi, cw, lane); break;
+            case 3: conv_pass<3>(tile, yr, yi, cw, lane); break;
+            case 4: conv_pass<4>(tile, yr, yi, cw, lane); break;
+            case 5: conv_pass<5>(tile, yr, yi, cw, lane); break;
+            default: conv_pass<6>(tile, yr, yi, cw, lane); break;
+          }
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[slot])) : "memory");
         }
-        fence_async_smem();
-        __syncwarp();
-        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[slot])) : "memory");
+        // the top three digits come from the high words, which are dead now:
+        // the next chunk's entries load during the other four passes
+        if (s == 2) load_chunk(i + 1);
       }
+      q += DIG;
+      if (!ok) break;
     }
   }
   tc_fence_before();
@@ -373,7 +434,7 @@ __global__ void bdigits_kernel(const double2* __restrict__ X, int64_t ldx, int k
     e = clamp_exp(col_exp[j]);
     if (k < kdim) x = X[(int64_t)k * ldx + j];
   }
-  const long long xr = __double2ll_rn(ldexp(x.x, 55 - e)), xi = __double2ll_rn(ldexp(x.y, 55 - e));
+  const long long xr = __double2ll_rn(ldexp(x.x, FIX - e)), xi = __double2ll_rn(ldexp(x.y, FIX - e));
   const long long yr = xr + BIAS, yi = xi + BIAS, yn = BIAS - xi;
   const int ctile = j / BNC, jj = j % BNC, c = k / KCC, kk = k % KCC;
   unsigned char* blk = out + ((size_t)ctile * nch + c) * B_BLOCK;

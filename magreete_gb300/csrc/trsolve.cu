@@ -65,11 +65,14 @@ diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* 
   const int r0 = i * kTB, rb = min(kTB, n - r0);
   for (int idx = tid; idx < kTB * kTB; idx += 256) {
     int r = idx >> 6, c = idx & 63;
-    Ts[r * (kTB + 1) + c] = (r < rb && c < rb) ? F[(int64_t)(r0 + r) * ldf + r0 + c] : czero<V>();
+    const bool ok = r < rb && c < rb;
+    cp_async_elem<(int)sizeof(V)>(Ts + r * (kTB + 1) + c, ok ? F + (int64_t)(r0 + r) * ldf + r0 + c : F, ok);
     V e = czero<V>();
     if (r == c) e.x = 1;
     Xs[r * kInvLd + c] = e;
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   if (UPPER)
     for (int r = tid; r < kTB; r += 256) dinv[r] = r < rb ? crecip(Ts[r * (kTB + 1) + r]) : czero<V>();
