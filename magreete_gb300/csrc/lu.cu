@@ -42,13 +42,13 @@ struct LuWsLayout {
   size_t slots = 64;      // 2 sets x 2*NBmax x int2 (pos, src)
   size_t records;         // 2 x kMaxPanelBlocks x kRecBytes
   size_t inv;             // 2 x NBmax x NBmax complex: inverses of a 128-wide block's diagonal blocks
-  size_t uinv;            // NBmax x NBmax complex64: U11^-1 of the last tile-pivoting panel
+  size_t uinv;            // NBmax x NBmax complex64: U11^-1, then L11^-1, of the last tile-pivoting panel
   size_t total;
   LuWsLayout() {
     records = (slots + 2 * 2 * kNBmax * sizeof(int2) + 127) & ~size_t(127);
     inv = records + 2 * (size_t)kMaxPanelBlocks * kRecBytes;
     uinv = inv + 2 * (size_t)kNBmax * kNBmax * sizeof(double2);
-    total = uinv + (size_t)kNBmax * kNBmax * sizeof(float2);
+    total = uinv + 2 * (size_t)kNBmax * kNBmax * sizeof(float2);
   }
 };
 
@@ -922,19 +922,23 @@ lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, 
   const int m = n - j0;
   const int ns = min(*ws.nslot, 2 * NB);
   // gather rows slot_src[q] (all slots: the top w rows are needed by the solve)
+  // asynchronous copies: every load of this stage in flight at once
   for (int idx = tid; idx < ns * kSwapCols; idx += blockDim.x) {
     int q = idx / kSwapCols, cc = idx - q * kSwapCols;
     int2 sl = ws.slots[q];
     bool inb = sl.x >= 0 && sl.x < m && sl.y >= 0 && sl.y < m;
     bool need = inb && ((sl.x != sl.y) || (right && sl.x < w));
-    if (cc < ncols && need) buf[q * kSwapCols + cc] = A[(int64_t)(j0 + sl.y) * lda + col0 + cc];
+    if (cc < ncols && need)
+      cp_async_elem<(int)sizeof(V)>(buf + q * kSwapCols + cc, A + (int64_t)(j0 + sl.y) * lda + col0 + cc, true);
   }
   if (right) {
     for (int idx = tid; idx < w * w; idx += blockDim.x) {
       int i = idx / w, k = idx - i * w;
-      L[i * NB + k] = A[(int64_t)(j0 + i) * lda + j0 + k];
+      cp_async_elem<(int)sizeof(V)>(L + i * NB + k, A + (int64_t)(j0 + i) * lda + j0 + k, true);
     }
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   if (right) {
     // 8 lanes per column: lane = col_local * 8 + t8, 4 columns per warp
@@ -977,16 +981,20 @@ lu_preupdate_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, in
   const int ncols = min(kSwapCols, n - col0);
   for (int idx = tid; idx < wb * kSwapCols; idx += 256) {
     int r = idx / kSwapCols, cc = idx - r * kSwapCols;
-    buf[r * kSwapCols + cc] = cc < ncols ? A[(int64_t)(j1 + r) * lda + col0 + cc] : czero<V>();
+    const bool ok = cc < ncols;
+    cp_async_elem<(int)sizeof(V)>(buf + r * kSwapCols + cc, ok ? A + (int64_t)(j1 + r) * lda + col0 + cc : A, ok);
   }
   for (int idx = tid; idx < wb * wa; idx += 256) {
     int r = idx / wa, k = idx - r * wa;
-    Lba[r * (NB + 1) + k] = A[(int64_t)(j1 + r) * lda + J0 + k];
+    cp_async_elem<(int)sizeof(V)>(Lba + r * (NB + 1) + k, A + (int64_t)(j1 + r) * lda + J0 + k, true);
   }
   for (int idx = tid; idx < wa * kSwapCols; idx += 256) {
     int k = idx / kSwapCols, cc = idx - k * kSwapCols;
-    Ua[k * kSwapCols + cc] = cc < ncols ? A[(int64_t)(J0 + k) * lda + col0 + cc] : czero<V>();
+    const bool ok = cc < ncols;
+    cp_async_elem<(int)sizeof(V)>(Ua + k * kSwapCols + cc, ok ? A + (int64_t)(J0 + k) * lda + col0 + cc : A, ok);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   // buf -= Lba * Ua: thread owns column cc = tid % 32 and rows tid / 32 + 8 q
   {
@@ -1100,19 +1108,22 @@ lu_block_right_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, int w
   const int nf = min(s_nf, MAXF);
   for (int f = tid; f < nf; f += blockDim.x) fsrc[f] = src_both(fpos[f]);
   __syncthreads();
-  // gather every source before anything is written
+  // gather every source before anything is written (asynchronous copies, all in flight)
   for (int idx = tid; idx < 2 * NB * CW; idx += blockDim.x) {
     const int r = idx / CW, c = idx - r * CW;
-    Tb[idx] = (r < W && c < ncols) ? A[(int64_t)(J0 + tsrc[r]) * lda + col0 + c] : czero<V>();
+    const bool ok = r < W && c < ncols;
+    cp_async_elem<(int)sizeof(V)>(Tb + idx, ok ? A + (int64_t)(J0 + tsrc[r]) * lda + col0 + c : A, ok);
   }
   for (int idx = tid; idx < nf * CW; idx += blockDim.x) {
     const int f = idx / CW, c = idx - f * CW;
-    if (c < ncols) Fr[idx] = A[(int64_t)(J0 + fsrc[f]) * lda + col0 + c];
+    if (c < ncols) cp_async_elem<(int)sizeof(V)>(Fr + idx, A + (int64_t)(J0 + fsrc[f]) * lda + col0 + c, true);
   }
   for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
     const int r = idx / NB, k = idx - r * NB;
-    Lb[r * (NB + 1) + k] = Inv[idx];
+    cp_async_elem<(int)sizeof(V)>(Lb + r * (NB + 1) + k, Inv + idx, true);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   for (int idx = tid; idx < nf * CW; idx += blockDim.x) {
     const int f = idx / CW, c = idx - f * CW;
@@ -1154,14 +1165,19 @@ lu_block_right_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int J0, int w
   if (wb > 0) {
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
       const int r = idx / NB, k = idx - r * NB;
-      Lb[r * (NB + 1) + k] = (r < wb && k < wa) ? A[(int64_t)(J0 + wa + r) * lda + J0 + k] : czero<V>();
+      const bool ok = r < wb && k < wa;
+      cp_async_elem<(int)sizeof(V)>(Lb + r * (NB + 1) + k, ok ? A + (int64_t)(J0 + wa + r) * lda + J0 + k : A, ok);
     }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     apply(NB, true);                                 // X_B -= L_BA U_A
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
       const int r = idx / NB, k = idx - r * NB;
-      Lb[r * (NB + 1) + k] = Inv[NB * NB + idx];
+      cp_async_elem<(int)sizeof(V)>(Lb + r * (NB + 1) + k, Inv + NB * NB + idx, true);
     }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     apply(NB, false);                                // U_B = L_BB^-1 X_B
   }
@@ -1251,73 +1267,165 @@ static int resolve_lu_options(const mgt_lu_options* o, LuOpts* r) {
 // swaps a few rows in a thousand there); the growth that remains is what
 // iterative refinement absorbs.
 constexpr int kTileLD = 65;   // padded row stride of the tile in shared memory
+// dynamic shared memory of lu_tile_kernel: the tile by row and by position,
+// two inversion scratch blocks, the staged candidate rows
+constexpr int kCandLD = 128;  // a staged candidate row: columns 4 (j + k) + g < 128
+constexpr size_t kTileSmem = (2 * 64 * kTileLD + 2 * 32 * 33 + 2 * 8 * kCandLD) * sizeof(float2);
 
+// In-place inverses of the upper triangle U (diagonal included) and of the
+// unit lower triangle L (strict lower part) of the 64 x 64 tile T, by block
+// recursion: for a block [[A, B], [0, C]] of U, the off-diagonal block of the
+// inverse is -(A^-1 B) C^-1; for [[A, 0], [B, C]] of L it is -C^-1 (B A^-1).
+// Level h combines 32 / h pairs of inverted h x h blocks; 256 threads.
+// A zero diagonal entry of U inverts to zero (the factorisation has already
+// recorded it as a zero pivot).
+__device__ void tile_triangular_inverses(float2* T, float2* S1, float2* S2, int tid) {
+  for (int i = tid; i < 64; i += 256) {
+    const float2 u = T[i * kTileLD + i];
+    T[i * kTileLD + i] = (u.x != 0.f || u.y != 0.f) ? crecip(u) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int h = 1; h < 64; h *= 2) {
+    const int nblk = 32 / h, per = h * h, tot = nblk * per;
+    // step 1: S1 = A^-1 B (upper), S2 = B A^-1 (lower); block q at rows / columns b = 2 h q
+    for (int e = tid; e < 2 * tot; e += 256) {
+      const bool up = e < tot;
+      const int f = up ? e : e - tot, q = f / per, i = (f % per) / h, j = f % h, b = 2 * h * q;
+      if (up) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = i; k < h; ++k) cfma(acc, T[(b + i) * kTileLD + b + k], T[(b + k) * kTileLD + b + h + j]);
+        S1[q * per + i * h + j] = acc;
+      } else {
+        // B: rows b + h .., columns b ..; A^-1 unit lower, (A^-1)[k][j] for k > j, diagonal 1
+        float2 acc = T[(b + h + i) * kTileLD + b + j];
+        for (int k = j + 1; k < h; ++k) cfma(acc, T[(b + h + i) * kTileLD + b + k], T[(b + k) * kTileLD + b + j]);
+        S2[q * per + i * h + j] = acc;
+      }
+    }
+    __syncthreads();
+    // step 2: B <- -(S1 C^-1) (upper), B <- -(C^-1 S2) (lower)
+    for (int e = tid; e < 2 * tot; e += 256) {
+      const bool up = e < tot;
+      const int f = up ? e : e - tot, q = f / per, i = (f % per) / h, j = f % h, b = 2 * h * q;
+      if (up) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = 0; k <= j; ++k) cfma(acc, S1[q * per + i * h + k], T[(b + h + k) * kTileLD + b + h + j]);
+        T[(b + i) * kTileLD + b + h + j] = make_float2(-acc.x, -acc.y);
+      } else {
+        float2 acc = S2[q * per + i * h + j];
+        for (int k = 0; k < i; ++k) cfma(acc, T[(b + h + i) * kTileLD + b + h + k], S2[q * per + k * h + j]);
+        T[(b + h + i) * kTileLD + b + j] = make_float2(-acc.x, -acc.y);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA of 256 threads; thread (r, g) = (tid / 4, tid % 4) holds the
+// columns g, g + 4, ... of tile row r in registers, a[k] = column 4 (j + k) + g
+// after j shifts (every fourth column), so register indices stay compile-time
+// constants and no loop has a data-dependent bound.  Per column c, with one
+// block barrier: the holders of column c bid |re| + |im| (lowest tile row on
+// ties); each warp's best row stages itself in cand[warp] before the barrier;
+// after it every thread reads the eight bids, the winner retires (its staged
+// row is row c of U), and the other rows compute their multiplier and update.
+// Rows never move between threads: the row chosen at column c goes to
+// position c, which gives the interchange slots directly.  Then all warps
+// invert U11 and L11 in place, for the rows below (L21 = A21 U11^-1) and the
+// columns to the right (U12 = L11^-1 A12).
 __global__ void __launch_bounds__(256)
 lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __restrict__ perm, PanelWs ws,
-               float2* __restrict__ Uinv) {
+               float2* __restrict__ Uinv, float2* __restrict__ Linv) {
   // A: the tile's top-left element (row j0, column j0); w <= 64
-  __shared__ float2 T[64 * kTileLD];
-  __shared__ float2 col[64];
+  extern __shared__ __align__(16) unsigned char tile_smem[];
+  float2* T = reinterpret_cast<float2*>(tile_smem);    // [64][kTileLD]: the tile, then the multipliers by tile row
+  float2* F = T + 64 * kTileLD;                         // [64][kTileLD], row q = position q
+  float2* S1 = F + 64 * kTileLD;
+  float2* S2 = S1 + 32 * 33;
+  float2* cand = S2 + 32 * 33;                          // [2][8][kCandLD]: each warp's best row, by column parity
+  __shared__ uint32_t s_key[2][8];
+  __shared__ int s_row[2][8];
   __shared__ int s_piv[64];
-  __shared__ int s_p;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < w * w; idx += 256) {
-    const int i = idx / w, k = idx - i * w;
-    T[i * kTileLD + k] = A[(int64_t)i * lda + k];
+  const int r = tid >> 2, g = tid & 3;
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int i = idx >> 6, k = idx & 63;
+    const bool in = i < w && k < w;
+    cp_async_elem<8>(T + i * kTileLD + k, in ? A + (int64_t)i * lda + k : A, in);
   }
+  cp_async_commit();
   if (tid < 64) s_piv[tid] = tid;
+  cp_async_wait<0>();
   __syncthreads();
-  for (int c = 0; c < w; ++c) {
-    if (warp == 0) {
-      // largest |re| + |im| among rows c .. w-1 of column c, lowest row on ties
-      uint32_t best = 0;
-      int bi = w;
-      for (int i = c + lane; i < w; i += 32) {
-        const float2 v = T[i * kTileLD + c];
-        const uint32_t key = __float_as_uint(fabsf(v.x) + fabsf(v.y));
-        if (bi == w || key > best) { best = key; bi = i; }
+  float2 a[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) a[k] = T[r * kTileLD + 4 * k + g];
+  bool active = r < w;
+  for (int j = 0; j < 16 && 4 * j < w; ++j) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int c = 4 * j + u;
+      if (c >= w) break;
+      const int buf = c & 1;
+      float2* cb = cand + buf * 8 * kCandLD;
+      // bid: key 0 = no bid; +1 keeps the rows of a zero column valid bidders
+      const uint32_t key = (active && g == u) ? __float_as_uint(fabsf(a[0].x) + fabsf(a[0].y)) + 1u : 0u;
+      const uint32_t mx = __reduce_max_sync(0xffffffffu, key);
+      const uint32_t ml = __reduce_min_sync(0xffffffffu, (key == mx && mx != 0u) ? (uint32_t)lane : 32u);
+      if (mx != 0u && (lane >> 2) == (int)(ml >> 2)) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cb[warp * kCandLD + 4 * (j + k) + g] = a[k];
       }
-      const uint32_t mx = __reduce_max_sync(0xffffffffu, best);
-      const int p = (int)__reduce_min_sync(0xffffffffu, (uint32_t)((bi < w && best == mx) ? bi : w));
-      if (lane == 0) s_p = p < w ? p : c;
-    }
-    __syncthreads();
-    const int p = s_p;
-    if (p != c) {
-      for (int k = tid; k < w; k += 256) {
-        const float2 t = T[c * kTileLD + k];
-        T[c * kTileLD + k] = T[p * kTileLD + k];
-        T[p * kTileLD + k] = t;
+      if (lane == 0) {
+        s_key[buf][warp] = mx;
+        s_row[buf][warp] = warp * 8 + (int)(ml >> 2);
       }
-      if (tid == 0) {
-        const int t = s_piv[c];
-        s_piv[c] = s_piv[p];
-        s_piv[p] = t;
-      }
-    }
-    __syncthreads();
-    const float2 piv = T[c * kTileLD + c];
-    if (piv.x == 0.f && piv.y == 0.f) {
-      // an exact zero pivot: recorded like LAPACK's info; the column stays as it is
-      if (tid == 0 && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
-    } else {
-      const float2 rp = crecip(piv);
-      for (int i = c + 1 + tid; i < w; i += 256) T[i * kTileLD + c] = cmul(T[i * kTileLD + c], rp);
       __syncthreads();
-      const int rem = w - c - 1;
-      for (int idx = tid; idx < rem * rem; idx += 256) {
-        const int i = c + 1 + idx / rem, k = c + 1 + idx % rem;
-        cfms(T[i * kTileLD + k], T[i * kTileLD + c], T[c * kTileLD + k]);
+      int best = 0;
+      uint32_t bk = s_key[buf][0];
+#pragma unroll
+      for (int q = 1; q < 8; ++q) {
+        const uint32_t kq = s_key[buf][q];
+        if (kq > bk) { bk = kq; best = q; }
+      }
+      const int p = s_row[buf][best];
+      const float2* prow = cb + best * kCandLD;
+      const float2 piv = prow[c];
+      if (tid < 64 && tid >= c) F[c * kTileLD + tid] = prow[tid];
+      if (r == p) {
+        if (g == 0) {
+          s_piv[c] = r;
+          if (piv.x == 0.f && piv.y == 0.f && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
+        }
+        active = false;
+      }
+      const bool nz = piv.x != 0.f || piv.y != 0.f;
+      float2 l = (g == u && nz) ? cmul(a[0], crecip(piv)) : make_float2(0.f, 0.f);
+      l.x = __shfl_sync(0xffffffffu, l.x, (lane & ~3) | u);
+      l.y = __shfl_sync(0xffffffffu, l.y, (lane & ~3) | u);
+      if (active) {
+        if (g == u) T[r * kTileLD + c] = l;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cfms(a[k], l, prow[4 * (j + k) + g]);
       }
     }
-    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 15; ++k) a[k] = a[k + 1];
   }
-  for (int idx = tid; idx < w * w; idx += 256) {
-    const int i = idx / w, k = idx - i * w;
-    A[(int64_t)i * lda + k] = T[i * kTileLD + k];
+  __syncthreads();
+  // the multipliers in position order (position q holds tile row s_piv[q]);
+  // identity beyond w (the last panel)
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int q = idx >> 6, k = idx & 63;
+    if (q >= w) F[q * kTileLD + k] = make_float2(q == k ? 1.f : 0.f, 0.f);
+    else if (k < q) F[q * kTileLD + k] = T[s_piv[q] * kTileLD + k];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int q = idx >> 6, k = idx & 63;
+    if (q < w && k < w) A[(int64_t)q * lda + k] = F[q * kTileLD + k];
   }
   if (warp == 0) {
-    // interchanges: position q of the tile holds the row that started at s_piv[q]
     for (int q = lane; q < kNBmax; q += 32) ws.slots[q] = make_int2(q, q < w ? s_piv[q] : q);
     if (lane == 0) *ws.nslot = kNBmax;
     int32_t pv[2];
@@ -1334,41 +1442,32 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
     }
   }
   __syncthreads();
-  // U11^-1 in place in the upper triangle of T, one column j at a time:
-  // x = U[0:j, j];  x <- -Uinv[0:j, 0:j] x / U[j][j]  (columns left of j are
-  // already inverted), then the diagonal
-  for (int j = 0; j < w; ++j) {
-    const float2 ujj = T[j * kTileLD + j];
-    const bool nz = ujj.x != 0.f || ujj.y != 0.f;
-    const float2 rj = nz ? crecip(ujj) : make_float2(0.f, 0.f);
-    if (tid < j) {
-      float2 acc = make_float2(0.f, 0.f);
-      for (int k = tid; k < j; ++k) cfma(acc, T[tid * kTileLD + k], T[k * kTileLD + j]);
-      col[tid] = cmul(acc, make_float2(-rj.x, -rj.y));
-    }
-    __syncthreads();
-    if (tid < j) T[tid * kTileLD + j] = col[tid];
-    if (tid == 0) T[j * kTileLD + j] = rj;
-    __syncthreads();
-  }
+  tile_triangular_inverses(F, S1, S2, tid);
   for (int idx = tid; idx < 64 * 64; idx += 256) {
     const int i = idx >> 6, k = idx & 63;
-    Uinv[idx] = (i < w && k < w && k >= i) ? T[i * kTileLD + k] : make_float2(0.f, 0.f);
+    const float2 v = F[i * kTileLD + k];
+    const bool inw = i < w && k < w;
+    Uinv[idx] = (inw && k >= i) ? v : make_float2(0.f, 0.f);
+    Linv[idx] = (inw && k < i) ? v : make_float2(i == k ? 1.f : 0.f, 0.f);
   }
 }
 
-// Rows below the tile: A21 <- A21 U11^-1 (w columns), 32 rows per CTA.
+// Rows below the tile: A21 <- A21 U11^-1 (w columns), 32 rows per CTA; the
+// operands are staged with asynchronous copies (all in flight at once).
 __global__ void __launch_bounds__(256)
 lu_l21_kernel(float2* __restrict__ A, int64_t lda, int rows, int w, const float2* __restrict__ Uinv) {
   // A: first row below the tile, first column of the panel
-  __shared__ float2 Ui[64 * 64];
-  __shared__ float2 Ar[32 * 64];
+  __shared__ __align__(16) float2 Ui[64 * 64];
+  __shared__ __align__(16) float2 Ar[32 * 64];
   const int tid = threadIdx.x, r0 = blockIdx.x * 32;
-  for (int idx = tid; idx < 64 * 64; idx += 256) Ui[idx] = Uinv[idx];
+  for (int idx = tid; idx < 64 * 32; idx += 256) cp_async_elem<16>(Ui + 2 * idx, Uinv + 2 * idx, true);
   for (int idx = tid; idx < 32 * 64; idx += 256) {
     const int r = idx >> 6, k = idx & 63;
-    Ar[idx] = (r0 + r < rows && k < w) ? A[(int64_t)(r0 + r) * lda + k] : make_float2(0.f, 0.f);
+    const bool in = r0 + r < rows && k < w;
+    cp_async_elem<8>(Ar + idx, in ? A + (int64_t)(r0 + r) * lda + k : A, in);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   const int r = tid >> 3, g = tid & 7;
   float2 acc[8];
@@ -1458,6 +1557,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
                          (int)((2 * NB * kSwapCols + NB * NB) * sizeof(V)));
     cudaFuncSetAttribute(lu_panel_reg_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)reg_panel_smem(NB, sizeof(V)));
+    cudaFuncSetAttribute(lu_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
   });
   PanelWs ws = panel_ws(work);
   if (cudaMemsetAsync(work, 0, 32, s) != cudaSuccess) return MGT_ERR_CUDA;   // status, nslot
@@ -1477,8 +1577,12 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   auto panel_only = [&](int j0, int w, int set) -> int {
     if constexpr (sizeof(T) == 4) {
       if (opt.pivoting == MGT_PIVOT_TILE) {
-        float2* Ui = reinterpret_cast<float2*>((char*)work + LuWsLayout().uinv);
-        lu_tile_kernel<<<1, 256, 0, s>>>(A + (int64_t)j0 * lda + j0, lda, w, j0, perm, panel_ws(work, set), Ui);
+        LuWsLayout Lw;
+        float2* Ui = reinterpret_cast<float2*>((char*)work + Lw.uinv);
+        // L11^-1 where the fused right-column pass reads the block's diagonal inverses
+        float2* Li = reinterpret_cast<float2*>((char*)work + Lw.inv) + (size_t)set * kNBmax * kNBmax;
+        lu_tile_kernel<<<1, 256, kTileSmem, s>>>(A + (int64_t)j0 * lda + j0, lda, w, j0, perm, panel_ws(work, set),
+                                                  Ui, Li);
         count_launch();
         const int below = n - j0 - w;
         if (below > 0) {
@@ -1635,7 +1739,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     if constexpr (sizeof(T) == 4) {
       if (wb > 0 && opt.fused_right) {
         V* Inv = reinterpret_cast<V*>((char*)work + LuWsLayout().inv);
-        lower_block_inverses<T>(A + (int64_t)J0 * lda + J0, lda, W, Inv, s);
+        // tile pivoting: the tile kernels left both diagonal blocks' inverses there
+        if (opt.pivoting != MGT_PIVOT_TILE) lower_block_inverses<T>(A + (int64_t)J0 * lda + J0, lda, W, Inv, s);
         lu_block_right_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, block_right_smem<NB>(sizeof(V)), s>>>(
             A, lda, n, J0, wa, wb, J0 + W, panel_ws(work, 0), panel_ws(work, 1), Inv);
         count_launch();
