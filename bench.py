@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--cfg4-fp64", action="store_true",
                     help="the large strong-scattering 3D case, mixed against the plain FP64 method (fields, DOS)")
     ap.add_argument("--cfg4-n", type=int, default=20000, help="with --cfg4-fp64: number of points")
+    ap.add_argument("--case", default=None, choices=sorted(KERNEL_CASES),
+                    help="run one small kernel workload twice and exit (the profiles' capture commands)")
     return ap.parse_args()
 
 
@@ -846,9 +848,51 @@ def run_cfg4_fp64(args):
     print(json.dumps(out), flush=True)
 
 
+# Small workloads of single kernels, each run twice (the second launch is the
+# one a profile captures): 3D dyadic N = 2000 (n = 6000) assembly and
+# tensor-core residual with 64 right-hand sides; the complex64 LU of 2D
+# N = 1000 (n = 2000) and 3D N = 4000 (n = 12000), tile or partial pivoting.
+KERNEL_CASES = ("assemble_3d_N2000", "residual_3d_N2000", "lu_2d_N1000_tile", "lu_2d_N1000_partial",
+                "lu_3d_N4000_tile", "lu_3d_N4000_partial")
+
+
+def run_case(name):
+    from magreete_gb300 import engine as E, selfterm
+    from magreete_gb300 import workloads as W
+    dev = torch.device("cuda")
+    if name.startswith("lu_"):
+        prob = W.cfg1() if "2d_N1000" in name else W.cfg2()
+    else:
+        prob = W.cube_problem(2000, 2, 10.0)
+    pts = prob.points.to(dev)
+    coef = prob.alpha * prob.k0 ** 2
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    if name == "assemble_3d_N2000":
+        for _ in range(2):
+            out = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf", "c64"))
+            torch.cuda.synchronize()
+            del out
+    elif name == "residual_3d_N2000":
+        (Mdf,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf",))
+        g = torch.Generator(device=dev).manual_seed(1)
+        X = torch.randn(prob.n, 64, dtype=torch.complex128, device=dev, generator=g)
+        B = torch.randn(prob.n, 64, dtype=torch.complex128, device=dev, generator=g)
+        for _ in range(2):
+            E.residual(Mdf, X, B)
+    else:
+        (M32,) = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("c64",))
+        for _ in range(2):
+            E.lu_factor(M32.clone(), check_singular=False, pivoting=name.rsplit("_", 1)[1])
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "ok": True}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.case:
+        run_case(args.case)
+        return
     if args.compare_fp64:
         run_compare_fp64(args)
         return

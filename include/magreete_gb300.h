@@ -203,7 +203,10 @@ int mgt_workspace_status(void* work, int32_t out[2], void* stream);
  * digits per entry (row / column power-of-two scales), digit pairs of equal
  * weight accumulate exactly in FP32 on tcgen05 and exactly in 64-bit
  * integers across K (error ~1e-14 of ||B|| on system matrices; within
- * n 2^-48 of |M||X| entry-wise).  A workspace of exactly n * nrhs * 16
+ * n 2^-48 of |M||X| entry-wise).  The workspace holds M's digits (14 bytes
+ * per entry, rows padded to 128, columns to 32), made by a pass over M in
+ * each call; mgt_solve_refined makes them once per solve and reuses them in
+ * every correction.  A workspace of exactly n * nrhs * 16
  * bytes (the double-float copy of X) selects double-float arithmetic on the
  * FP32 pipes (products exact via fma, sums compensated), unsplit.  Used by
  * iterative refinement.
@@ -212,6 +215,18 @@ int mgt_residual_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
 int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X, int64_t ldx,
                  const void* B, int64_t ldb, void* R, int64_t ldr, int64_t nrhs,
                  void* work, size_t work_bytes, void* stream);
+
+/*
+ * The two halves of mgt_residual on its workspace (mgt_residual_workspace_bytes
+ * for the largest nrhs to be applied): mgt_residual_prepare makes M's row
+ * exponents and digits there; mgt_residual_apply then computes R = B - M X
+ * from them, for any number of X while M is unchanged.  Stream-ordered: an
+ * apply sees the prepare enqueued before it on the same stream.
+ * MGT_ERR_UNSUPPORTED where the tensor-core residual is unavailable.
+ */
+int mgt_residual_prepare(const void* M, int64_t n, int64_t ldm, void* work, size_t work_bytes, void* stream);
+int mgt_residual_apply(int64_t n, const void* X, int64_t ldx, const void* B, int64_t ldb, void* R, int64_t ldr,
+                       int64_t nrhs, void* work, size_t work_bytes, void* stream);
 
 /*
  * Mixed-precision solve of M X = B: complex64 LU factors of M (from
@@ -233,7 +248,8 @@ int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int64_t ldlu,
  * synchronise with the host, so a whole refined solve can be captured into a
  * CUDA graph (the batched sweep does).  Same workspace as mgt_solve_refined.
  *   mgt_refine_start:   X = LU^-1 B (complex64 solve, widened to complex128)
- *   mgt_refine_correct: X += LU^-1 (B - M X), residual in double-float
+ *   mgt_refine_correct: X += LU^-1 (B - M X), residual as in mgt_residual
+ *                       (M's digits are made again in each call)
  *   mgt_refine_norms:   norms_dev[0] = ||B||_F^2, norms_dev[1] = ||B - M X||_F^2
  *                       (device doubles; the caller reads them when it syncs)
  */

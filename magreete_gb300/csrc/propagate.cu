@@ -295,7 +295,7 @@ extern "C" int mgt_propagate(int kind, int dtype, const double* targets, int64_t
       if (e != MGT_OK) break;
       const double2* b = E0 ? (const double2*)E0 + t0 * d * ld_e0 : nullptr;
       e = residual_tc(Gc, (int64_t)d * ns, tc * d, d * ns, (const double2*)Ek, ld_ek, (int)nrhs, b, ld_e0,
-                      (double2*)out + t0 * d * ld_out, ld_out, nullptr, tw, tw_bytes, st);
+                      (double2*)out + t0 * d * ld_out, ld_out, tw, tw_bytes, st);
     }
     return e;
   }

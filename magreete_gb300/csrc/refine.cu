@@ -290,7 +290,8 @@ struct RefineWs {
   double2* part;  // (double-float residual) split-K partial sums
   int64_t part_elems;
   int* rowexp;    // (tensor-core residual) row exponents of M
-  void* tcw;      // (tensor-core residual) its workspace
+  unsigned char* digits;   // (tensor-core residual) digits of M
+  void* tcw;      // (tensor-core residual) one application's workspace
   size_t tcw_bytes;
   size_t total;
   RefineWs(void* base, int64_t n, int64_t r) {
@@ -307,12 +308,15 @@ struct RefineWs {
     part = nullptr;
     part_elems = 0;
     rowexp = nullptr;
+    digits = nullptr;
     tcw = nullptr;
     tcw_bytes = 0;
     if (tc) {
       rowexp = (int*)take(n * sizeof(int));
       off = (off + 1023) & ~size_t(1023);
-      tcw_bytes = residual_tc_workspace_bytes(n, n, r);
+      digits = (unsigned char*)take(residual_tc_digits_bytes(n, n));
+      off = (off + 1023) & ~size_t(1023);
+      tcw_bytes = residual_tc_apply_bytes(n, n, r);
       tcw = take(tcw_bytes);
     } else {
       Xs = (float4*)take(n * r * sizeof(float4));
@@ -321,15 +325,16 @@ struct RefineWs {
     }
     total = off;
   }
-  // Rr = B - M X; rowexp_ready: the row exponents of this M are in rowexp
+  // Rr = B - M X; prepared: the row exponents and digits of this M are in
+  // the workspace already (made by an earlier residual of the same solve)
   int residual(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb, int n,
-               int nr, bool rowexp_ready, cudaStream_t s) {
+               int nr, bool prepared, cudaStream_t s) {
     if (tc) {
-      if (!rowexp_ready) {
-        int e = residual_tc_rowexp(M, ldm, n, n, rowexp, s);
+      if (!prepared) {
+        int e = residual_tc_prepare(M, ldm, n, n, rowexp, digits, s);
         if (e != MGT_OK) return e;
       }
-      return residual_tc(M, ldm, n, n, X, ldx, nr, B, ldb, Rr, nr, rowexp, tcw, tcw_bytes, s);
+      return residual_tc_apply(digits, rowexp, n, n, X, ldx, nr, B, ldb, Rr, nr, tcw, tcw_bytes, s);
     }
     return residual_impl(M, ldm, X, ldx, B, ldb, Rr, nr, n, nr, Xs, part, part_elems, s);
   }
@@ -362,7 +367,7 @@ extern "C" int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X
   // tensor cores when the workspace holds their buffers
   if (residual_tc_supported(n, n, nrhs) && work_bytes >= residual_tc_workspace_bytes(n, n, nrhs))
     return residual_tc((const float4*)M, ldm, (int)n, (int)n, (const double2*)X, ldx, (int)nrhs, (const double2*)B,
-                       ldb, (double2*)R, ldr, nullptr, work, work_bytes, (cudaStream_t)stream);
+                       ldb, (double2*)R, ldr, work, work_bytes, (cudaStream_t)stream);
   if (work_bytes < (size_t)n * nrhs * sizeof(float4)) return MGT_ERR_WORKSPACE;
   // split-K partials after the double-float copy of X, as far as the workspace holds them
   const size_t xs_bytes = ((size_t)n * nrhs * sizeof(float4) + 255) & ~size_t(255);
@@ -374,6 +379,31 @@ extern "C" int mgt_residual(const void* M, int64_t n, int64_t ldm, const void* X
   }
   return residual_impl((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, (double2*)R, ldr,
                        (int)n, (int)nrhs, (float4*)work, part, part_elems, (cudaStream_t)stream);
+}
+
+extern "C" int mgt_residual_prepare(const void* M, int64_t n, int64_t ldm, void* work, size_t work_bytes,
+                                    void* stream) {
+  if (!M || !work || n <= 0 || ldm < n) return MGT_ERR_ARG;
+  if (n > (1 << 30)) return MGT_ERR_WORKSPACE;
+  if (!residual_tc_supported(n, n, 1)) return MGT_ERR_UNSUPPORTED;
+  int* rowexp;
+  unsigned char* digits;
+  if (work_bytes < residual_tc_split(work, n, n, &rowexp, &digits, nullptr)) return MGT_ERR_WORKSPACE;
+  return residual_tc_prepare((const float4*)M, ldm, (int)n, (int)n, rowexp, digits, (cudaStream_t)stream);
+}
+
+extern "C" int mgt_residual_apply(int64_t n, const void* X, int64_t ldx, const void* B, int64_t ldb, void* R,
+                                  int64_t ldr, int64_t nrhs, void* work, size_t work_bytes, void* stream) {
+  if (!X || !B || !R || !work || n <= 0 || nrhs <= 0 || ldx < nrhs || ldb < nrhs || ldr < nrhs) return MGT_ERR_ARG;
+  if (n > (1 << 30)) return MGT_ERR_WORKSPACE;
+  if (!residual_tc_supported(n, n, nrhs)) return MGT_ERR_UNSUPPORTED;
+  if (work_bytes < residual_tc_workspace_bytes(n, n, nrhs)) return MGT_ERR_WORKSPACE;
+  int* rowexp;
+  unsigned char* digits;
+  char* aw;
+  const size_t a_off = residual_tc_split(work, n, n, &rowexp, &digits, &aw);
+  return residual_tc_apply(digits, rowexp, (int)n, (int)n, (const double2*)X, ldx, (int)nrhs, (const double2*)B, ldb,
+                           (double2*)R, ldr, aw, work_bytes - a_off, (cudaStream_t)stream);
 }
 
 extern "C" int mgt_refine_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes) {

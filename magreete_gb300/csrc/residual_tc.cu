@@ -29,31 +29,33 @@
 //    integer.
 //  * Every 128 real K the level sums are read out of TMEM and folded into
 //    one 64-bit integer per output in units of 2^-48 of the row and column
-//    scales: levels 0 .. 4 exactly, 5 and 6 rounded to the nearest unit.  A
-//    64-bit accumulator per output in shared memory sums them exactly (at
-//    most 2^15 real K per CTA keeps it below 2^63); the result is scaled back
-//    once at the end.
+//    scales: levels 0 .. 4 exactly, 5 and 6 rounded to within 0.53 unit.  A
+//    64-bit accumulator per output sums them exactly (at most 2^15 real K per
+//    CTA keeps it below 2^63); the result is scaled back once at the end.
 // Accuracy (a numpy emulation of exactly this scheme on 2D / 3D systems of
 // order 1400 / 2100): residual errors of 3e-14 / 1e-14 of ||B||, where six
 // digits give 8e-12 / 2e-12.
 //
-// Kernel: one CTA per (128 rows) x (32 complex right-hand sides) x (a range
-// of K in 32-column chunks), 512 threads:
-//   warp 0     : bulk copies of the right-hand sides' digit blocks (made by
-//                bdigits_kernel in the layout shared memory needs), 2 stages
-//   warp 1     : MMA issuer.  Per chunk and digit s of A', one MMA per
-//                16-wide K step covers the levels s .. 6 at once: the seven
-//                digit slices of B' are stacked along N, so the levels s + t,
-//                t = 0 .. 6 - s, are adjacent TMEM columns (N <= 256 per MMA:
-//                10 MMAs per K step instead of 28, A read once per MMA)
-//   warp 2     : TMEM allocation (7 levels x 64 columns)
-//   warps 4-7  : epilogue, thread = row: level sums -> 64-bit accumulators
-//   warps 8-23 : converters, eight rows each: the double-float entries of M
-//                are loaded for a whole chunk at once, turned into 54-bit
-//                integers, and their digits (one byte permute, one logic op
-//                and one fp16 subtract per re / im pair) written straight
-//                into the 128-byte-swizzled K-major layout of the MMA's A
-//                operand, one digit slice at a time through a ring
+// Two passes.  digitize_kernel turns M into its digits once per matrix
+// (refinement reuses them for every residual): one byte per digit (the
+// biased digit d + 128), seven digit slices of 128 rows x 64 real K per
+// (row tile, 32-column chunk), 56 KB contiguous, each slice laid out as the
+// MMA operand's 128-byte-swizzled K-major rows at half width, so that
+// widening byte k of a slice to fp16 lands at byte 2k of the operand.
+// residual_tc_kernel: one CTA per (32 complex right-hand sides) x (128 rows)
+// x (a range of K in chunks), 512 threads:
+//   warp 0      : TMEM allocation (7 levels x 64 columns); bulk copies: per chunk the right-hand sides' digit block
+//                 (bdigits_kernel, 56 KB, 2 stages) and the seven 8 KB digit
+//                 slices of M (6-slice ring), whichever has a free slot
+//   warp 1      : MMA issuer.  Per chunk and digit s of A', one MMA per
+//                 16-wide K step covers the levels s .. 6 at once: the seven
+//                 digit slices of B' are stacked along N, so the levels
+//                 s + t, t = 0 .. 6 - s, are adjacent TMEM columns (N <= 256
+//                 per MMA: 10 MMAs per K step instead of 28)
+//   warps 2-9   : epilogue: thread = (row, half of the 64 real columns);
+//                 level sums -> 64-bit accumulators in registers
+//   warps 10-15 : converters: a staged byte slice -> the fp16 operand slice
+//                 (one byte permute and one fp16 subtract per digit pair)
 // Every wait is bounded; a CTA whose wait runs out writes NaN outputs, sets
 // MGT_ERR_TIMEOUT in the status word, drains what it issued and returns.
 #include <cuda_fp16.h>
@@ -74,22 +76,27 @@ constexpr int BNC = 32;                 // complex right-hand sides per tile
 constexpr int BN = 2 * BNC;             // real columns per tile (TMEM columns per level)
 constexpr int KCC = 32;                 // complex K per chunk (64 real: one 128-byte fp16 row)
 constexpr int DIG = 7;                  // digits per operand
-constexpr int ASLOTS = 3;               // A digit-slice ring
-constexpr uint32_t A_SLICE = BM * 128;              // 16 KB
+constexpr int ASLOTS = 4;               // fp16 operand-slice ring
+constexpr int DSLOTS = 6;               // byte-slice staging ring
+constexpr uint32_t A_SLICE = BM * 128;              // 16 KB: one fp16 digit slice of A'
+constexpr uint32_t D_SLICE = BM * 64;               // 8 KB: the same slice, one byte per digit
 constexpr uint32_t B_SLICE = BN * 128;              // 8 KB
 constexpr uint32_t B_BLOCK = DIG * B_SLICE;         // 56 KB: one chunk of B', all digit slices
-constexpr uint32_t W_BYTES = BM * BN * 8;           // 64-bit accumulators
 constexpr uint32_t TMEM_COLS = 512;
-constexpr int NCONV = 16, NEPI = 4;
-constexpr int THREADS = (4 + NEPI + NCONV) * 32;
-constexpr int ROWS_PER_CONV = BM / NCONV;           // 8
+constexpr int NEPI = 8, NCONV = 6;
+constexpr int EPI0 = 2;                             // first epilogue warp
+// 16 warps: four per SM sub-partition leave 128 registers per thread
+constexpr int THREADS = (EPI0 + NEPI + NCONV) * 32;
+constexpr int EPI_COLS = BN / (NEPI / 4);           // real columns per epilogue thread
 // at most 512 chunks (32768 real K) per CTA: |sum| <= 2^15 * 2^48 = 2^63
 // units of 2^-48, less the rounding of levels 5 and 6
 constexpr int MAX_SPLIT_CHUNKS = 512;
 constexpr long long BIAS = 0x0080808080808080LL;    // 128 in each of the seven digit positions
 constexpr int FIX = 54;                             // |X| < 2^FIX
 
-constexpr size_t smem_bytes() { return 1024 + ASLOTS * A_SLICE + 2 * B_BLOCK + W_BYTES + BM * sizeof(int) + 256; }
+constexpr size_t smem_bytes() {
+  return 1024 + ASLOTS * A_SLICE + DSLOTS * D_SLICE + 2 * B_BLOCK + BM * sizeof(int) + 256;
+}
 
 // round(f * 2^sh) as a 64-bit integer (|f| * 2^sh < 2^54 by the row scale);
 // zero and subnormal f (below 2^-126) give 0
@@ -121,25 +128,16 @@ __device__ __forceinline__ float digit_f(long long y, int p) {
   return __int_as_float(0x4B400000 | (int)byte) - 12583040.0f;   // byte - 128
 }
 
-// fp16 pair (digit P of yr, digit P of yi) as one 32-bit word: the two bytes
-// are picked by one byte permute, turned into the fp16 encodings of
-// 1024 + byte, and 1152 is subtracted (byte - 128, exact)
-template <int P>
-__device__ __forceinline__ uint32_t digit_pair(long long yr, long long yi) {
-  const uint32_t wr = P < 4 ? (uint32_t)yr : (uint32_t)((unsigned long long)yr >> 32);
-  const uint32_t wi = P < 4 ? (uint32_t)yi : (uint32_t)((unsigned long long)yi >> 32);
-  constexpr uint32_t b = P & 3;
-  const uint32_t x = __byte_perm(wr, wi, b | (b << 4) | ((4 + b) << 8) | ((4 + b) << 12));
-  const uint32_t h = (x & 0x00FF00FFu) | 0x64006400u;
+// Four biased digit bytes b0..b3 -> two fp16 pairs (b0 - 128, b1 - 128),
+// (b2 - 128, b3 - 128): a byte permute places each byte under 0x64 (the fp16
+// encoding of 1024 + byte), and 1152 is subtracted (exact).
+__device__ __forceinline__ uint2 widen4(uint32_t x) {
+  const uint32_t h0 = __byte_perm(x, 0x64646464u, 0x4140), h1 = __byte_perm(x, 0x64646464u, 0x4342);
   const __half2 c = __halves2half2(__ushort_as_half((unsigned short)0x6480), __ushort_as_half((unsigned short)0x6480));
-  const __half2 d = __hsub2(*reinterpret_cast<const __half2*>(&h), c);
-  return *reinterpret_cast<const uint32_t*>(&d);
+  const __half2 d0 = __hsub2(*reinterpret_cast<const __half2*>(&h0), c);
+  const __half2 d1 = __hsub2(*reinterpret_cast<const __half2*>(&h1), c);
+  return make_uint2(*reinterpret_cast<const uint32_t*>(&d0), *reinterpret_cast<const uint32_t*>(&d1));
 }
-
-// one digit slice of a converter warp's rows: row cw + NCONV t, lane = complex column
-template <int P>
-__device__ __forceinline__ void conv_pass(unsigned char* tile, const long long (&yr)[ROWS_PER_CONV],
-                                          const long long (&yi)[ROWS_PER_CONV], int cw, int lane);
 
 // row exponent of a row holding a NaN or an infinity: its outputs are NaN
 constexpr int kRowNonFinite = 0x40000000;
@@ -153,16 +151,8 @@ __device__ __forceinline__ uint32_t swz(int rho, int kr) {
   return (uint32_t)rho * 128u + ((uint32_t)(((kr >> 3) ^ (rho & 7)) << 4)) + (uint32_t)((kr & 7) * 2);
 }
 
-template <int P>
-__device__ __forceinline__ void conv_pass(unsigned char* tile, const long long (&yr)[ROWS_PER_CONV],
-                                          const long long (&yi)[ROWS_PER_CONV], int cw, int lane) {
-#pragma unroll
-  for (int t = 0; t < ROWS_PER_CONV; ++t)
-    *reinterpret_cast<uint32_t*>(tile + swz(cw + NCONV * t, 2 * lane)) = digit_pair<P>(yr[t], yi[t]);
-}
-
 __global__ void __launch_bounds__(THREADS, 1)
-residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim, const int* __restrict__ row_exp,
+residual_tc_kernel(const unsigned char* __restrict__ D, int rows, const int* __restrict__ row_exp,
                    const int* __restrict__ col_exp, const unsigned char* __restrict__ bdig, int nch_total, int ncols,
                    int chunks_per_split, const double2* __restrict__ B, int64_t ldb, double2* __restrict__ R,
                    int64_t ldr, double2* __restrict__ partial, int* status) {
@@ -171,11 +161,13 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* aring = base;
   unsigned char* bring = aring + ASLOTS * A_SLICE;
-  long long* wacc = reinterpret_cast<long long*>(bring + 2 * B_BLOCK);   // [BN][BM]
-  int* rexp = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(wacc) + W_BYTES);
+  unsigned char* dring = bring + 2 * B_BLOCK;
+  int* rexp = reinterpret_cast<int*>(dring + DSLOTS * D_SLICE);
   uint64_t* full_a = reinterpret_cast<uint64_t*>(rexp + BM);
   uint64_t* empty_a = full_a + ASLOTS;
-  uint64_t* full_b = empty_a + ASLOTS;
+  uint64_t* full_d = empty_a + ASLOTS;
+  uint64_t* empty_d = full_d + DSLOTS;
+  uint64_t* full_b = empty_d + DSLOTS;
   uint64_t* empty_b = full_b + 2;
   uint64_t* tfull = empty_b + 2;
   uint64_t* tempty = tfull + 1;
@@ -184,7 +176,7 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row0 = blockIdx.x * BM, ct = blockIdx.y, sp = blockIdx.z;
+  const int ct = blockIdx.x, rt = blockIdx.y, sp = blockIdx.z, row0 = rt * BM;
   const int c_begin = sp * chunks_per_split;
   const int nchunk = max(0, min(nch_total, c_begin + chunks_per_split) - c_begin);
   const int nread = (nchunk + 1) >> 1;
@@ -192,6 +184,7 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
   if (threadIdx.x < BM) rexp[threadIdx.x] = (row0 + (int)threadIdx.x < rows) ? clamp_exp(row_exp[row0 + threadIdx.x]) : 0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < ASLOTS; ++s) { mbar_init(&full_a[s], NCONV); mbar_init(&empty_a[s], 1); }
+    for (int s = 0; s < DSLOTS; ++s) { mbar_init(&full_d[s], 1); mbar_init(&empty_d[s], NCONV); }
     for (int s = 0; s < 2; ++s) { mbar_init(&full_b[s], 1); mbar_init(&empty_b[s], 1); }
     mbar_init(tfull, 1);
     mbar_init(tempty, NEPI);
@@ -199,7 +192,7 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) {
+  if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(TMEM_COLS)
                  : "memory");
@@ -211,16 +204,35 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // ---------------- producer: digit blocks of B' for each chunk
-    int i = 0;
-    for (; i < nchunk && !*abort; ++i) {
-      const int st = i & 1;
-      if (i >= 2 && !mbar_wait(&empty_b[st], ((i >> 1) - 1) & 1, abort)) break;
-      mbar_expect_tx(&full_b[st], B_BLOCK);
-      bulk_load(bring + st * B_BLOCK, bdig + ((size_t)ct * nch_total + c_begin + i) * B_BLOCK, B_BLOCK, &full_b[st]);
+    // ---------------- producer: digit blocks of B', digit slices of A'.
+    // Whichever copy has a free slot is issued (B blocks first), so a B
+    // block goes out as soon as the MMAs of the block two back have completed
+    // rather than behind the slices of the current chunk.
+    const unsigned char* dsrc = D + ((size_t)rt * nch_total + c_begin) * DIG * D_SLICE;
+    const int nq = nchunk * DIG;
+    int ib = 0, q = 0;
+    uint32_t idle = 0;
+    while ((ib < nchunk || q < nq) && !*abort) {
+      bool progress = false;
+      if (ib < nchunk && (ib < 2 || mbar_try_wait(&empty_b[ib & 1], ((ib >> 1) - 1) & 1))) {
+        mbar_expect_tx(&full_b[ib & 1], B_BLOCK);
+        bulk_load(bring + (ib & 1) * B_BLOCK, bdig + ((size_t)ct * nch_total + c_begin + ib) * B_BLOCK, B_BLOCK,
+                  &full_b[ib & 1]);
+        ++ib;
+        progress = true;
+      }
+      if (q < nq && (q < DSLOTS || mbar_try_wait(&empty_d[q % DSLOTS], ((q / DSLOTS) - 1) & 1))) {
+        mbar_expect_tx(&full_d[q % DSLOTS], D_SLICE);
+        bulk_load(dring + (q % DSLOTS) * D_SLICE, dsrc + (size_t)q * D_SLICE, D_SLICE, &full_d[q % DSLOTS]);
+        ++q;
+        progress = true;
+      }
+      if (progress) idle = 0;
+      else if (++idle >= kWaitLimit) { *abort = 1; break; }
     }
     // copies in flight land before the CTA may exit
-    for (int j = max(0, i - 2); j < i; ++j) mbar_wait_plain(&full_b[j & 1], (j >> 1) & 1);
+    for (int j = max(0, ib - 2); j < ib; ++j) mbar_wait_plain(&full_b[j & 1], (j >> 1) & 1);
+    for (int j = max(0, q - DSLOTS); j < q; ++j) mbar_wait_plain(&full_d[j % DSLOTS], (j / DSLOTS) & 1);
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
     int q = 0;
@@ -257,37 +269,46 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
       if (!first || i == nchunk - 1) mma_commit(tfull);
     }
     mma_commit(done);   // arrives once every MMA issued above has completed
-  } else if (warp >= 4 && warp < 4 + NEPI) {
-    // ---------------- epilogue: thread = row of the tile
-    const int qd = warp - 4, r = qd * 32 + lane;
-    for (int j = 0; j < BN; ++j) wacc[j * BM + r] = 0;
-    const uint32_t tbase = tmem + ((uint32_t)(qd * 32) << 16);
+  } else if (warp >= EPI0 && warp < EPI0 + NEPI) {
+    // ---------------- epilogue: thread = (row, half of the real columns)
+    // a warp reads the TMEM lanes of its rank modulo 4
+    const int qd = warp & 3, part = (warp - EPI0) >> 2, r = qd * 32 + lane;
+    long long acc[EPI_COLS];
+#pragma unroll
+    for (int j = 0; j < EPI_COLS; ++j) acc[j] = 0;
+    const uint32_t tbase = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(part * EPI_COLS);
     bool ok = true;
     for (int ro = 0; ro < nread; ++ro) {
       if (!mbar_wait(tfull, ro & 1, abort)) { ok = false; break; }
       tc_fence_after();
-#pragma unroll 1
-      for (int p = 0; p < BN / 8; ++p) {
-        uint32_t v[DIG][8];
+      // a fresh copy per readout keeps the 28 TMEM addresses from being
+      // hoisted out of the loop into registers
+      uint32_t tb;
+      asm volatile("mov.b32 %0, %1;" : "=r"(tb) : "r"(tbase));
 #pragma unroll
-        for (int l = 0; l < DIG; ++l) tmem_ld8(tbase + (uint32_t)(l * BN + p * 8), v[l]);
+      for (int p = 0; p < EPI_COLS / 4; ++p) {
+        uint32_t v[DIG][4];
+#pragma unroll
+        for (int l = 0; l < DIG; ++l) tmem_ld4(tb + (uint32_t)(l * BN + p * 4), v[l]);
         tmem_wait_ld();
-        if (p == BN / 8 - 1) {
+        if (p == EPI_COLS / 4 - 1) {
           tc_fence_before();
           __syncwarp();
           if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tempty)) : "memory");
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          // level l weighs 2^(36 - 8 l) units of 2^-48
-          const long long low = ((long long)__float2int_rz(__uint_as_float(v[5][j])) << 8) +
-                                (long long)__float2int_rz(__uint_as_float(v[6][j]));
-          const long long w = ((long long)__float2int_rz(__uint_as_float(v[0][j])) << 36) +
-                              ((long long)__float2int_rz(__uint_as_float(v[1][j])) << 28) +
-                              ((long long)__float2int_rz(__uint_as_float(v[2][j])) << 20) +
-                              ((long long)__float2int_rz(__uint_as_float(v[3][j])) << 12) +
-                              ((long long)__float2int_rz(__uint_as_float(v[4][j])) << 4) + ((low + 2048) >> 12);
-          wacc[(p * 8 + j) * BM + r] += w;
+        for (int j = 0; j < 4; ++j) {
+          // level l weighs 2^(36 - 8 l) units of 2^-48.  With |L_0| <= 2^19,
+          // |L_1| <= 2^21, |L_2| <= 2^22, |L_3| < 2^22.6, |L_4| <= 2^23 (top
+          // digits at most 64): hi = L_0 2^8 + L_1 and mid = L_2 2^8 + L_3 are
+          // exact in 32 bits; levels 5 and 6 round to the nearest unit through
+          // one FMA ((L_5 + L_6 / 256) / 16, its own rounding below 1/32 unit)
+          const int hi = (__float2int_rz(__uint_as_float(v[0][j])) << 8) + __float2int_rz(__uint_as_float(v[1][j]));
+          const int mid = (__float2int_rz(__uint_as_float(v[2][j])) << 8) + __float2int_rz(__uint_as_float(v[3][j]));
+          const int l4 = __float2int_rz(__uint_as_float(v[4][j]));
+          const int l56 = __float2int_rn(
+              0.0625f * fmaf(__uint_as_float(v[6][j]), 0.00390625f, __uint_as_float(v[5][j])));
+          acc[p * 4 + j] += ((long long)hi << 28) + ((long long)mid << 12) + (long long)((l4 << 4) + l56);
         }
       }
     }
@@ -295,80 +316,58 @@ residual_tc_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim
     if (row < rows) {
       const bool good = ok && !*abort && row_exp[row] != kRowNonFinite;
       const int ea = rexp[r];
-      for (int jc = 0; jc < BNC; ++jc) {
-        const int col = ct * BNC + jc;
-        if (col >= ncols) break;
-        double2 val;
-        if (good) {
-          const int sc = ea + clamp_exp(col_exp[col]) - 48;
-          val = make_double2(ldexp((double)wacc[(2 * jc) * BM + r], sc), ldexp((double)wacc[(2 * jc + 1) * BM + r], sc));
-        } else {
-          val = make_double2(__longlong_as_double(0x7FF8000000000000LL), __longlong_as_double(0x7FF8000000000000LL));
-        }
-        if (partial) {
-          partial[((int64_t)sp * rows + row) * ncols + col] = val;
-        } else {
-          const double2 b = B ? B[(int64_t)row * ldb + col] : make_double2(0.0, 0.0);
-          R[(int64_t)row * ldr + col] = make_double2(b.x - val.x, b.y - val.y);
+#pragma unroll
+      for (int jc = 0; jc < EPI_COLS / 2; ++jc) {
+        const int col = ct * BNC + part * (EPI_COLS / 2) + jc;
+        if (col < ncols) {
+          double2 val;
+          if (good) {
+            // 2^sc, sc in [-648, 552]: a normal double
+            const double sc = __longlong_as_double((long long)(ea + clamp_exp(col_exp[col]) - 48 + 1023) << 52);
+            val = make_double2((double)acc[2 * jc] * sc, (double)acc[2 * jc + 1] * sc);
+          } else {
+            val = make_double2(__longlong_as_double(0x7FF8000000000000LL),
+                               __longlong_as_double(0x7FF8000000000000LL));
+          }
+          if (partial) {
+            partial[((int64_t)sp * rows + row) * ncols + col] = val;
+          } else {
+            const double2 b = B ? B[(int64_t)row * ldb + col] : make_double2(0.0, 0.0);
+            R[(int64_t)row * ldr + col] = make_double2(b.x - val.x, b.y - val.y);
+          }
         }
       }
     }
-  } else if (warp >= 4 + NEPI) {
-    // ---------------- converters: rows cw, cw + NCONV, ...; lane = complex column of the chunk
-    const int cw = warp - 4 - NEPI;
-    int q = 0;
-    float4 v[ROWS_PER_CONV];
-    auto load_chunk = [&](int i) {
-      const int kc = (c_begin + i) * KCC + lane;
-#pragma unroll
-      for (int t = 0; t < ROWS_PER_CONV; ++t) {
-        const int row = row0 + cw + NCONV * t;
-        v[t] = (i < nchunk && row < rows && kc < kdim) ? __ldg(&M[(int64_t)row * ldm + kc])
-                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+  } else if (warp >= EPI0 + NEPI) {
+    // ---------------- converters: staged byte slice -> fp16 operand slice
+    const int ctid = threadIdx.x - (EPI0 + NEPI) * 32;
+    const int nq = nchunk * DIG;
+    for (int q = 0; q < nq; ++q) {
+      const int ds = q % DSLOTS, as = q % ASLOTS;
+      if (!mbar_wait(&full_d[ds], (q / DSLOTS) & 1, abort)) break;
+      if (q >= ASLOTS && !mbar_wait(&empty_a[as], ((q / ASLOTS) - 1) & 1, abort)) break;
+      const unsigned char* src = dring + ds * D_SLICE;
+      unsigned char* dst = aring + as * A_SLICE;
+      // thread: 8 digit bytes -> 16 contiguous operand bytes (both accesses
+      // contiguous across the warp)
+      for (int u = ctid; u < (int)(D_SLICE / 8); u += NCONV * 32) {
+        const uint32_t off = (uint32_t)u * 8u;
+        const uint2 v = *reinterpret_cast<const uint2*>(src + off);
+        const uint2 w0 = widen4(v.x), w1 = widen4(v.y);
+        *reinterpret_cast<uint4*>(dst + 2 * off) = make_uint4(w0.x, w0.y, w1.x, w1.y);
       }
-    };
-    load_chunk(0);
-    for (int i = 0; i < nchunk && !*abort; ++i) {
-      long long yr[ROWS_PER_CONV], yi[ROWS_PER_CONV];
-#pragma unroll
-      for (int t = 0; t < ROWS_PER_CONV; ++t) {
-        const int sh = FIX - rexp[cw + NCONV * t];
-        yr[t] = fixed_point(v[t].x, sh) + fixed_low(v[t].y, sh) + BIAS;
-        yi[t] = fixed_point(v[t].z, sh) + fixed_low(v[t].w, sh) + BIAS;
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[as])) : "memory");
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty_d[ds])) : "memory");
       }
-      bool ok = true;
-#pragma unroll
-      for (int s = 0; s < DIG; ++s) {
-        const int slot = (q + s) % ASLOTS;
-        if (ok && q + s >= ASLOTS && !mbar_wait(&empty_a[slot], (((q + s) / ASLOTS) - 1) & 1, abort)) ok = false;
-        if (ok) {
-          unsigned char* tile = aring + slot * A_SLICE;
-          switch (DIG - 1 - s) {
-            case 0: conv_pass<0>(tile, yr, yi, cw, lane); break;
-            case 1: conv_pass<1>(tile, yr, yi, cw, lane); break;
-            case 2: conv_pass<2>(tile, yr, yi, cw, lane); break;
-            case 3: conv_pass<3>(tile, yr, yi, cw, lane); break;
-            case 4: conv_pass<4>(tile, yr, yi, cw, lane); break;
-            case 5: conv_pass<5>(tile, yr, yi, cw, lane); break;
-            default: conv_pass<6>(tile, yr, yi, cw, lane); break;
-          }
-          fence_async_smem();
-          __syncwarp();
-          if (lane == 0)
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[slot])) : "memory");
-        }
-        // the top three digits come from the high words, which are dead now:
-        // the next chunk's entries load during the other four passes
-        if (s == 2) load_chunk(i + 1);
-      }
-      q += DIG;
-      if (!ok) break;
     }
   }
   tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0 && *abort) atomicExch(status, MGT_ERR_TIMEOUT);
-  if (warp == 2) {
+  if (warp == 0) {
     // every issued MMA has completed before the accumulator columns are freed
     if (lane == 0) mbar_wait_plain(done, 0);
     __syncwarp();
@@ -392,6 +391,48 @@ __global__ void rowexp_kernel(const float4* __restrict__ M, int64_t ldm, int row
   if (m >= 0x7F800000u) e = kRowNonFinite;
   else if (m != 0u) frexpf(__uint_as_float(m), &e);
   if (lane == 0) out[row] = e;
+}
+
+// Byte p (0 = lowest) of each of four 64-bit words, packed low to high.
+__device__ __forceinline__ uint32_t pick_bytes(const long long* y, int p) {
+  const int b = p & 3;
+  uint32_t w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) w[k] = p < 4 ? (uint32_t)y[k] : (uint32_t)((unsigned long long)y[k] >> 32);
+  const uint32_t sel = (uint32_t)(b | ((4 + b) << 4));
+  return __byte_perm(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel), 0x5410);
+}
+
+// Digits of M (the A' operand) for every (row tile, chunk): block
+// (rt, c) holds slices s = 0 .. 6 (digit p = 6 - s), 8 KB each, byte
+// (rho, kr) of a slice at rho * 64 + (((kr >> 3) ^ (rho & 7)) << 3) + (kr & 7):
+// the swizzled fp16 operand layout at half width.  Zeros beyond rows and kdim.
+// Thread = (row, 8 real K = 4 complex entries), four per thread.
+__global__ void __launch_bounds__(256)
+digitize_kernel(const float4* __restrict__ M, int64_t ldm, int rows, int kdim, const int* __restrict__ row_exp,
+                unsigned char* __restrict__ D, int nch) {
+  const int c = blockIdx.x, rt = blockIdx.y;
+  unsigned char* blk = D + ((size_t)rt * nch + c) * DIG * D_SLICE;
+#pragma unroll 1
+  for (int t = threadIdx.x; t < BM * 8; t += 256) {
+    const int rho = t >> 3, grp = t & 7, row = rt * BM + rho;
+    const bool rin = row < rows;
+    const int sh = FIX - (rin ? clamp_exp(row_exp[row]) : 0);
+    long long y[8];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int kc = c * KCC + grp * 4 + e;
+      const float4 v = (rin && kc < kdim) ? __ldg(&M[(int64_t)row * ldm + kc]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      y[2 * e] = fixed_point(v.x, sh) + fixed_low(v.y, sh) + BIAS;
+      y[2 * e + 1] = fixed_point(v.z, sh) + fixed_low(v.w, sh) + BIAS;
+    }
+    const uint32_t off = (uint32_t)rho * 64u + ((uint32_t)(grp ^ (rho & 7)) << 3);
+#pragma unroll
+    for (int s = 0; s < DIG; ++s) {
+      const int p = DIG - 1 - s;
+      *reinterpret_cast<uint2*>(blk + s * D_SLICE + off) = make_uint2(pick_bytes(y, p), pick_bytes(y + 4, p));
+    }
+  }
 }
 
 // f_j of each right-hand side: 2^f_j bounds the column's largest |re|, |im|.
@@ -479,9 +520,9 @@ static void plan_splits(int rows, int kdim, int ncols, int* splits, int* cps) {
   *splits = (nch + c - 1) / c;
 }
 
+// workspace of one application (the digits of M are the caller's)
 struct TcResWs {
   int* status;
-  int* rowexp;
   int* colexp;
   unsigned char* bdig;
   double2* partial;
@@ -500,13 +541,14 @@ struct TcResWs {
     nch = (kdim + KCC - 1) / KCC;
     ctiles = (ncols + BNC - 1) / BNC;
     status = (int*)take(256, 256);
-    rowexp = (int*)take((size_t)rows * sizeof(int), 256);
     colexp = (int*)take((size_t)ncols * sizeof(int), 256);
     bdig = (unsigned char*)take((size_t)ctiles * nch * B_BLOCK, 1024);
     partial = splits > 1 ? (double2*)take((size_t)splits * rows * ncols * sizeof(double2), 256) : nullptr;
     total = off + 256;
   }
 };
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace rtc
 
@@ -515,22 +557,41 @@ bool residual_tc_supported(int64_t rows, int64_t kdim, int64_t ncols) {
          ncols <= (1 << 16);
 }
 
-size_t residual_tc_workspace_bytes(int64_t rows, int64_t kdim, int64_t ncols) {
+size_t residual_tc_digits_bytes(int64_t rows, int64_t kdim) {
+  using namespace rtc;
+  return (size_t)((rows + BM - 1) / BM) * (size_t)((kdim + KCC - 1) / KCC) * DIG * D_SLICE;
+}
+
+size_t residual_tc_apply_bytes(int64_t rows, int64_t kdim, int64_t ncols) {
   if (!residual_tc_supported(rows, kdim, ncols)) return 0;
   return rtc::TcResWs(nullptr, (int)rows, (int)kdim, (int)ncols).total;
 }
 
-int residual_tc_rowexp(const float4* M, int64_t ldm, int rows, int kdim, int* out, cudaStream_t s) {
-  count_launch();
-  rtc::rowexp_kernel<<<(rows + 7) / 8, 256, 0, s>>>(M, ldm, rows, kdim, out);
+size_t residual_tc_workspace_bytes(int64_t rows, int64_t kdim, int64_t ncols) {
+  using namespace rtc;
+  if (!residual_tc_supported(rows, kdim, ncols)) return 0;
+  return align_up((size_t)rows * sizeof(int), 1024) + align_up(residual_tc_digits_bytes(rows, kdim), 1024) +
+         residual_tc_apply_bytes(rows, kdim, ncols);
+}
+
+int residual_tc_prepare(const float4* M, int64_t ldm, int rows, int kdim, int* rowexp, unsigned char* digits,
+                        cudaStream_t s) {
+  using namespace rtc;
+  if (!residual_tc_supported(rows, kdim, 1)) return MGT_ERR_UNSUPPORTED;
+  if (!M || !rowexp || !digits || ((uintptr_t)digits & 15)) return MGT_ERR_ARG;
+  const int nch = (kdim + KCC - 1) / KCC;
+  count_launch(2);
+  rowexp_kernel<<<(rows + 7) / 8, 256, 0, s>>>(M, ldm, rows, kdim, rowexp);
+  digitize_kernel<<<dim3(nch, (rows + BM - 1) / BM), 256, 0, s>>>(M, ldm, rows, kdim, rowexp, digits, nch);
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
-int residual_tc(const float4* M, int64_t ldm, int rows, int kdim, const double2* X, int64_t ldx, int ncols,
-                const double2* B, int64_t ldb, double2* R, int64_t ldr, const int* rowexp, void* work,
-                size_t work_bytes, cudaStream_t s) {
+int residual_tc_apply(const unsigned char* digits, const int* rowexp, int rows, int kdim, const double2* X,
+                      int64_t ldx, int ncols, const double2* B, int64_t ldb, double2* R, int64_t ldr, void* work,
+                      size_t work_bytes, cudaStream_t s) {
   using namespace rtc;
   if (!residual_tc_supported(rows, kdim, ncols)) return MGT_ERR_UNSUPPORTED;
+  if (!digits || !rowexp || ((uintptr_t)digits & 15)) return MGT_ERR_ARG;
   TcResWs w(work, rows, kdim, ncols);
   if (!work || work_bytes < w.total) return MGT_ERR_WORKSPACE;
   static OncePerDevice once;
@@ -538,11 +599,6 @@ int residual_tc(const float4* M, int64_t ldm, int rows, int kdim, const double2*
     cudaFuncSetAttribute(residual_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes());
   });
   if (cudaMemsetAsync(w.status, 0, sizeof(int), s) != cudaSuccess) return MGT_ERR_CUDA;
-  if (!rowexp) {
-    int e = residual_tc_rowexp(M, ldm, rows, kdim, w.rowexp, s);
-    if (e != MGT_OK) return e;
-    rowexp = w.rowexp;
-  }
   // column exponents start far below any real one (0x80808080)
   if (cudaMemsetAsync(w.colexp, 0x80, (size_t)ncols * sizeof(int), s) != cudaSuccess) return MGT_ERR_CUDA;
   count_launch(2);
@@ -550,8 +606,10 @@ int residual_tc(const float4* M, int64_t ldm, int rows, int kdim, const double2*
   const int64_t nb = (int64_t)w.nch * KCC * w.ctiles * BNC;
   bdigits_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(X, ldx, kdim, ncols, w.colexp, w.bdig, w.nch, w.ctiles);
   count_launch();
-  dim3 grid((rows + BM - 1) / BM, w.ctiles, w.splits);
-  residual_tc_kernel<<<grid, THREADS, smem_bytes(), s>>>(M, ldm, rows, kdim, rowexp, w.colexp, w.bdig, w.nch, ncols,
+  // column tiles of one row tile are neighbours in the launch order, so the
+  // second reads the row tile's digit slices from L2
+  dim3 grid(w.ctiles, (rows + BM - 1) / BM, w.splits);
+  residual_tc_kernel<<<grid, THREADS, smem_bytes(), s>>>(digits, rows, rowexp, w.colexp, w.bdig, w.nch, ncols,
                                                            w.cps, B, ldb, R, ldr, w.partial, w.status);
   if (w.splits > 1) {
     const int64_t tot = (int64_t)rows * ncols;
@@ -560,5 +618,31 @@ int residual_tc(const float4* M, int64_t ldm, int rows, int kdim, const double2*
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
+
+size_t residual_tc_split(void* work, int64_t rows, int64_t kdim, int** rowexp, unsigned char** digits, char** aw) {
+  using namespace rtc;
+  char* b = (char*)work;
+  const size_t d_off = align_up((size_t)rows * sizeof(int), 1024);
+  const size_t a_off = d_off + align_up(residual_tc_digits_bytes(rows, kdim), 1024);
+  if (rowexp) *rowexp = (int*)b;
+  if (digits) *digits = (unsigned char*)(b + d_off);
+  if (aw) *aw = b + a_off;
+  return a_off;
+}
+
+int residual_tc(const float4* M, int64_t ldm, int rows, int kdim, const double2* X, int64_t ldx, int ncols,
+                const double2* B, int64_t ldb, double2* R, int64_t ldr, void* work, size_t work_bytes,
+                cudaStream_t s) {
+  if (!residual_tc_supported(rows, kdim, ncols)) return MGT_ERR_UNSUPPORTED;
+  if (!work || work_bytes < residual_tc_workspace_bytes(rows, kdim, ncols)) return MGT_ERR_WORKSPACE;
+  int* rowexp;
+  unsigned char* digits;
+  char* aw;
+  const size_t a_off = residual_tc_split(work, rows, kdim, &rowexp, &digits, &aw);
+  int e = residual_tc_prepare(M, ldm, rows, kdim, rowexp, digits, s);
+  if (e != MGT_OK) return e;
+  return residual_tc_apply(digits, rowexp, rows, kdim, X, ldx, ncols, B, ldb, R, ldr, aw, work_bytes - a_off, s);
+}
+
 
 }  // namespace mgt

@@ -236,6 +236,34 @@ def residual(Mdf, X, B):
     return Rr
 
 
+class ResidualOperator:
+    """R = B - M X for a fixed double-float M and any number of X (up to
+    max_nrhs columns each): M's digits are made once (mgt_residual_prepare)
+    and every call applies them (mgt_residual_apply, tensor cores only)."""
+
+    def __init__(self, Mdf, max_nrhs):
+        self.lib = L.load()
+        self.n = Mdf.shape[0]
+        self.max_nrhs = max_nrhs
+        nb = ctypes.c_size_t()
+        L.check(self.lib.mgt_residual_workspace_bytes(self.n, max_nrhs, ctypes.byref(nb)),
+                "mgt_residual_workspace_bytes")
+        self.work = workspace(nb.value, Mdf.device)
+        L.check(self.lib.mgt_residual_prepare(_ptr(Mdf), self.n, self.n, _ptr(self.work), self.work.numel(),
+                                              _stream()), "mgt_residual_prepare")
+
+    def __call__(self, X, B):
+        n, R = B.shape
+        if n != self.n or R > self.max_nrhs:
+            raise ValueError(f"shape {tuple(B.shape)} does not fit an operator of order {self.n} "
+                             f"with at most {self.max_nrhs} right-hand sides")
+        X, B = X.contiguous(), B.contiguous()
+        Rr = torch.empty_like(B)
+        L.check(self.lib.mgt_residual_apply(n, _ptr(X), R, _ptr(B), R, _ptr(Rr), R, R, _ptr(self.work),
+                                            self.work.numel(), _stream()), "mgt_residual_apply")
+        return Rr
+
+
 # ------------------------------------------------------------------ system solve
 
 def solve_system(kind, points, k0, coef, shift, E0, precision="fp64", tol=DEFAULT_TOL,

@@ -79,14 +79,19 @@ def matrix_bytes(prob, precision="mixed"):
     tensor-core split buffers (3 KB per row), the right-hand-side blocks and
     the propagation workspace (double-float propagator rows, at most 1 GiB at
     a time, and the double-float copy of the fields), the split-K partial sums
-    of the residual (at most 16 splits) and the digit blocks of the
-    tensor-core residual (56 KB per 32 rows and 32 right-hand sides)."""
+    of the residual (at most 16 splits) and the digits of the tensor-core
+    residual: the right-hand sides' (56 KB per 32 rows and 32 right-hand
+    sides) and, in the mixed method, the matrix's (14 B per entry, rows padded
+    to 128) and the propagator rows' (14 B per entry of a chunk)."""
     n, R = prob.n, prob.nrhs
     per = 16 if precision == "fp64" else 24
     T = prob.detectors.shape[0] if prob.detectors is not None else 0
-    prop = min(1 << 30, 16 * prob.d * n * T) + 16 * n * R
+    chunk = min(1 << 30, 16 * prob.d * n * T)
+    prop = chunk + 16 * n * R + (chunk * 14 // 16 if precision != "fp64" else 0)
     partial = 16 * 16 * n * max(R, 64)
     digits = 57344 * -(-n // 32) * -(-R // 32)
+    if precision != "fp64":
+        digits += 14 * (-(-n // 128) * 128) * (-(-n // 32) * 32)
     return per * n * n + 3072 * n + 8 * 16 * n * R + prop + partial + digits + (64 << 20)
 
 

@@ -72,6 +72,8 @@ def test_invalid_arguments_rejected_before_any_device_work():
     assert lib.mgt_lu_factor_static(L.MGT_C64, null, 100, 100, null, null, null) == ARG
     assert lib.mgt_lu_solve(L.MGT_C64, null, 100, 100, null, null, 4, null, 4, 4, null, 0, null) == ARG
     assert lib.mgt_residual(null, 100, 100, null, 4, null, 4, null, 4, 4, null, 0, null) == ARG
+    assert lib.mgt_residual_prepare(null, 100, 100, null, 0, null) == ARG
+    assert lib.mgt_residual_apply(100, null, 4, null, 4, null, 4, 4, null, 0, null) == ARG
     assert lib.mgt_solve_refined(null, 100, null, 100, null, 100, null, 4, null, 4, 4, 1e-10, 10, null, 0,
                                  None, None, null) == ARG
     assert lib.mgt_refine_start(null, 100, null, 100, null, 4, null, 4, 4, null, 0, null) == ARG

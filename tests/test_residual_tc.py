@@ -101,3 +101,18 @@ def test_refinement_uses_tc_residual_and_converges():
     assert st["rel_residual"] <= 1e-10
     X64 = E.solve_system(prob.kind, pts, prob.k0, coef, shift, Bv, "fp64")
     assert (torch.linalg.norm(X - X64) / torch.linalg.norm(X64)).item() < 1e-8
+
+
+def test_prepared_operator_matches_one_shot_residual():
+    """mgt_residual_prepare once, mgt_residual_apply for several X (fewer
+    columns than prepared for, too): bit-identical to mgt_residual."""
+    from magreete_gb300 import engine as E
+    M, Mdf, gen = _system(900, "3d_vector", 11)
+    n = M.shape[0]
+    op = E.ResidualOperator(Mdf, 40)
+    for R in (40, 7):
+        X = torch.randn(n, R, dtype=torch.complex128, generator=gen).cuda()
+        B = torch.randn(n, R, dtype=torch.complex128, generator=gen).cuda()
+        assert torch.equal(op(X, B), E.residual(Mdf, X, B))
+    with pytest.raises(ValueError):
+        op(X[:, :1].repeat(1, 41), B[:, :1].repeat(1, 41))
