@@ -412,21 +412,28 @@ def secondary_rooflines():
     gen = torch.Generator(device=dev).manual_seed(5)
     X = torch.randn(n, R, dtype=torch.complex128, device=dev, generator=gen)
     B = torch.randn(n, R, dtype=torch.complex128, device=dev, generator=gen)
+    op = E.ResidualOperator(Mdf, R)
     for _ in range(2):
-        E.residual(Mdf, X, B)
+        op(X, B)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 5
     e0.record()
     for _ in range(reps):
-        E.residual(Mdf, X, B)
+        op(X, B)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    e0.record()
+    for _ in range(reps):
+        E.residual(Mdf, X, B)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_call = e0.elapsed_time(e1) / reps
     tflop = 224.0 * n * n * R / 1e12
-    nbytes = 16.0 * n * n + 3 * 16.0 * n * R
-    out["residual_tc"] = {"kernel": "rtc::residual_tc_kernel (+ row / column scales, right-hand-side digits, "
-                                    "reduction of the K splits)",
+    nbytes = 14.0 * n * n + 3 * 16.0 * n * R
+    out["residual_tc"] = {"kernel": "rtc::residual_tc_kernel (+ the right-hand sides' scales and digits, reduction "
+                                    "of the K splits); M's digits made beforehand (mgt_residual_prepare)",
                           "bound": "tensor", "n": n, "nrhs": R, "ms": ms,
                           "achieved": tflop / (ms * 1e-3), "peak": bf16, "unit": "TFLOP/s",
                           "frac": tflop / (ms * 1e-3) / bf16,
@@ -435,8 +442,10 @@ def secondary_rooflines():
                           "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / hbm,
                           "peak_source": f"bf16_tflops of {src} peaks (kind::f16 runs at the bf16 rate); "
                                          "224 n^2 R flops = 28 digit-pair products of the 7-digit split",
-                          "complex_macs_per_s": float(n) * n * R / (ms * 1e-3)}
-    del Mdf, X, B
+                          "complex_macs_per_s": float(n) * n * R / (ms * 1e-3),
+                          "one_call_ms_with_digit_pass": ms_call,
+                          "measured": "CUDA events over 5 applications of mgt_residual_apply, after 2"}
+    del Mdf, X, B, op
     prob = W.cfg1()
     pts = prob.points.to(dev)
     coef = prob.alpha * prob.k0 ** 2
@@ -820,23 +829,31 @@ def run_cfg4_fp64(args):
     out = {"case": f"3D ball N={prob.N} (n={prob.n}), n_ref 2.0, k0L 2pi*15, {prob.nrhs} RHS, "
                    f"{det.shape[0]} detectors; mean DOS at {len(mp)} points"}
     res = {}
+    P = mp.shape[0]
     for prec in ("mixed", "fp64"):
+        # one factorisation per method serves the fields and the DOS (the
+        # classes' solve and mean_DOS_measurements would each factor: at this
+        # size one FP64 LU takes minutes)
         s = Transmission3D_vector(pts, source="plane", precision=prec)
         E0s = s.generate_source(pts, prob.k0, prob.u, prob.p, 0.2)
         E0d = s.generate_source(det, prob.k0, prob.u, prob.p, 0.2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Ek = s.solve(prob.k0, prob.alpha, prob.radius, E0s)
+        fac = s._factorization(prob.k0, prob.alpha, prob.radius, True, "Rayleigh")
+        Ek = fac.solve(E0s.reshape(prob.n, -1).to(torch.complex128))
         Ed = s.propagate(det, Ek, prob.k0, prob.alpha, E0d)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        dos = float(s.mean_DOS_measurements(mp.to(dev), prob.k0, prob.alpha, prob.radius))
+        dots = s._dos_terms(fac, mp.to(dev), prob.k0, prob.radius, True, "Rayleigh", False)
+        dos = float(torch.imag(dots.sum() / P * complex(s._DOS_PREF[s.kind](prob.k0, prob.alpha))))
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         res[prec] = (Ek.cpu(), Ed.cpu(), dos)
-        out[prec] = {"solve_propagate_s": t1 - t0, "mean_dos_s": t2 - t1, "stats": dict(s.last_stats),
-                     "mean_dos": dos}
-        del Ek, Ed, s
+        out[prec] = {"factor_solve_propagate_s": t1 - t0, "mean_dos_s": t2 - t1, "mean_dos": dos,
+                     "refine_iterations": getattr(fac, "last_iterations", 0),
+                     "rel_residual": getattr(fac, "last_residual", None),
+                     "pivoting": getattr(getattr(fac, "f", None), "pivoting", None)}
+        del Ek, Ed, s, fac, dots
         torch.cuda.empty_cache()
     (Em, Dm, dm), (Ef, Df, df) = res["mixed"], res["fp64"]
     col = lambda a, b: (torch.linalg.norm(a - b, dim=0) / torch.linalg.norm(b, dim=0)).max().item()

@@ -235,8 +235,18 @@ int mgt_residual_apply(int64_t n, const void* X, int64_t ldx, const void* B, int
  * X (complex128) receives the solution.  iters / rel_res (host pointers,
  * may be NULL) receive the number of corrections and the final relative
  * residual.  Returns MGT_ERR_NOT_CONVERGED if tol was not met.
+ *
+ * mgt_refine_prepare makes M's digits (the tensor-core residual's operand)
+ * in a refinement workspace of mgt_refine_workspace_bytes(n, nrhs) bytes, so
+ * that M itself may be freed: mgt_solve_refined, mgt_refine_correct and
+ * mgt_refine_norms then take M = NULL and use the prepared digits, for any
+ * nrhs up to the one prepared for (stream-ordered, like every call here).
+ * MGT_ERR_UNSUPPORTED where the tensor-core residual is unavailable; M = NULL
+ * without tensor cores is MGT_ERR_ARG.
  */
 int mgt_refine_workspace_bytes(int64_t n, int64_t nrhs, size_t* bytes);
+int mgt_refine_prepare(const void* M, int64_t ldm, int64_t n, int64_t nrhs, void* work, size_t work_bytes,
+                       void* stream);
 int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int64_t ldlu,
                       const int32_t* perm, int64_t n, const void* B, int64_t ldb,
                       void* X, int64_t ldx, int64_t nrhs, double tol, int max_iter,

@@ -70,6 +70,7 @@ SIGNATURES = {
     "mgt_residual_workspace_bytes": (_i32, [_i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_residual": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_residual_prepare": (_i32, [_vp, _i64, _i64, _vp, _sz, _vp]),
+    "mgt_refine_prepare": (_i32, [_vp, _i64, _i64, _i64, _vp, _sz, _vp]),
     "mgt_residual_apply": (_i32, [_i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _sz, _vp]),
     "mgt_refine_workspace_bytes": (_i32, [_i64, _i64, ctypes.POINTER(_sz)]),
     "mgt_solve_refined": (_i32, [_vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _f64, _i32, _vp, _sz,

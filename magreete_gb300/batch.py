@@ -84,6 +84,15 @@ class _Instance:
         L.check(lib.mgt_assemble_system(E.KIND_CODE[p.kind], _ptr(self.pts), p.N, float(p.k0), coef.real, coef.imag,
                                         shift.real, shift.imag, _ptr(self.Mdf), n, L.MGT_CDF, _ptr(self.M32),
                                         self.M32.stride(0), L.MGT_C64, stream_ptr), "mgt_assemble_system")
+        # M's digits for every residual of this solve (corrections and norms
+        # then pass no matrix); the double-float matrix itself where the
+        # tensor-core residual is unavailable
+        st = lib.mgt_refine_prepare(_ptr(self.Mdf), n, n, R, _ptr(self.rw), self.rw.numel(), stream_ptr)
+        if st == L.MGT_ERR_UNSUPPORTED:
+            self.mref = _ptr(self.Mdf)
+        else:
+            L.check(st, "mgt_refine_prepare")
+            self.mref = None
         opt = options if options is not None else self.lu_options
         L.check(lib.mgt_lu_factor_ex(L.MGT_C64, _ptr(self.M32), n, self.M32.stride(0), _ptr(self.perm),
                                      _ptr(self.luw), self.luw.numel(), ctypes.byref(opt), stream_ptr),
@@ -98,14 +107,14 @@ class _Instance:
     def correct(self, lib, stream_ptr):
         p = self.prob
         n, R = p.n, p.nrhs
-        L.check(lib.mgt_refine_correct(_ptr(self.Mdf), n, _ptr(self.M32), self.M32.stride(0), _ptr(self.perm), n,
+        L.check(lib.mgt_refine_correct(self.mref, n, _ptr(self.M32), self.M32.stride(0), _ptr(self.perm), n,
                                        _ptr(self.B), R, _ptr(self.X), R, R, _ptr(self.rw), self.rw.numel(),
                                        stream_ptr), "mgt_refine_correct")
 
     def measure(self, lib, stream_ptr):
         p = self.prob
         n, R = p.n, p.nrhs
-        L.check(lib.mgt_refine_norms(_ptr(self.Mdf), n, n, _ptr(self.B), R, _ptr(self.X), R, R, _ptr(self.rw),
+        L.check(lib.mgt_refine_norms(self.mref, n, n, _ptr(self.B), R, _ptr(self.X), R, R, _ptr(self.rw),
                                      self.rw.numel(), ctypes.c_void_p(self.norms.data_ptr()), stream_ptr),
                 "mgt_refine_norms")
 

@@ -24,15 +24,18 @@
 // (column's) largest flush to zero, an absolute error below that of FP32
 // rounding of the row's largest entry.
 //
-// Kernel: one CTA per 128 x 128 tile of C' (128 rows, 64 complex columns).
+// Kernel: persistent, one CTA per SM walking 128 x 128 tiles of C' (128 rows,
+// 64 complex columns):
 //   warp 0 lane 0 : TMA producer (cp.async.bulk.tensor, 128B swizzle) of the
-//                   A_hi/A_lo (128 x 32 fp32) and B_hi/B_lo (256 x 32 fp32)
-//                   tiles of each 32-wide K block, 2-stage mbarrier ring
-//   warp 1 lane 0 : tcgen05.mma issuer (M=128, N=256, K=8 per instruction,
-//                   12 instructions per K block), tcgen05.commit to free a
-//                   stage and, at the end, to publish the accumulator
-//   warp 2        : TMEM allocation / deallocation (256 columns)
-//   warps 4-7     : epilogue: tcgen05.ld 32 columns at a time, C -= acc
+//                   A_hi/A_lo (128 rows) and B_hi/B_lo (128 rows of B'^T)
+//                   tiles of each K block (one 128-byte row: 64 fp16 or 32
+//                   fp32), 3-stage mbarrier ring
+//   warp 1 lane 0 : tcgen05.mma issuer (M = 128, N = 128, 32 bytes of K per
+//                   instruction, 12 instructions per K block), tcgen05.commit
+//                   to free a stage and, at the end, to publish the accumulator
+//   warp 2        : TMEM allocation / deallocation (2 accumulators x 128 columns)
+//   warp 3 lane 0 : C mover: TMA reduce-adds of 128 x 32 chunks into C
+//   warps 4-7     : epilogue: tcgen05.ld 32 columns at a time, -acc staged
 // Every wait is bounded; on expiry the CTA records MGT_ERR_TIMEOUT, drains
 // the MMAs it issued, frees its TMEM and returns.
 #include <cuda.h>
@@ -63,7 +66,7 @@ constexpr int CHUNKS = BN / 32;            // epilogue chunks per tile (32 fp32 
 constexpr uint32_t CHUNK_BYTES = BM * 128; // 16 KB
 constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int THREADS = 256;
-// pipeline shape: operand stages x C ring slots (2 x 4: 128 + 64 KB)
+// pipeline shape: operand stages x C ring slots (3 x 2: 192 + 32 KB)
 template <int STAGES, int CSLOTS>
 constexpr size_t smem_bytes() {
   return STAGES * STAGE_BYTES + CSLOTS * CHUNK_BYTES + 1024 /* alignment slack */ + 256;
@@ -95,23 +98,12 @@ __device__ __forceinline__ void mma_split(uint32_t d_tmem, uint64_t a, uint64_t 
         : "memory");
   }
 }
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-// named barrier over the 128 epilogue threads that also ANDs a predicate
-__device__ __forceinline__ bool epi_bar_and(bool p) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 1, 128, pi;\n selp.u32 %0, 1, 0, po;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)p)
-      : "memory");
-  return r != 0;
-}
-
 // Persistent kernel: each CTA walks tiles blockIdx.x, +gridDim.x, ...; TMEM
 // holds two accumulators so the epilogue of tile t overlaps the MMAs of
-// tile t+1; C moves through a ring of 128 x 32 fp32 chunks with TMA loads
-// (prefetched CSLOTS - 1 chunks ahead) and TMA stores, a slot being refilled
-// once the store issued before the newest one has read it.
+// tile t+1.  C is never loaded into the SM: the epilogue stages -acc in a
+// ring of 128 x 32 fp32 chunks and one C-mover thread adds each chunk into C
+// with a TMA reduce (f32 add at L2), handing a slot back once its reduce has
+// read it.
 // invA / invB (F16 mode): inverse row scales of A and inverse complex-column
 // scales of B, relative to the block being updated.
 template <bool F16, int STAGES, int CSLOTS>
@@ -128,16 +120,17 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;
   uint64_t* tempty = tfull + 2;
-  uint64_t* cfull = tempty + 2;
-  uint64_t* done = cfull + CSLOTS;
+  uint64_t* cfree = tempty + 2;
+  uint64_t* cdone = cfree + CSLOTS;
+  uint64_t* done = cdone + CSLOTS;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int a = 0; a < 2; ++a) { mbar_init(&tfull[a], 1); mbar_init(&tempty[a], 4); }
-    for (int c = 0; c < CSLOTS; ++c) mbar_init(&cfull[c], 1);
+    for (int a = 0; a < 2; ++a) { mbar_init(&tfull[a], 1); mbar_init(&tempty[a], 128); }
+    for (int c = 0; c < CSLOTS; ++c) { mbar_init(&cfree[c], 1); mbar_init(&cdone[c], 128); }
     mbar_init(done, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -201,37 +194,49 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
       if (!ok) break;
     }
     mma_commit(done);   // arrives once every MMA this thread issued has completed
-  } else if (warp >= 4) {
-    // ---------------- epilogue: 128 threads, thread = accumulator row
-    const int q = warp - 4, r = q * 32 + lane;
-    const bool leader = (q == 0 && lane == 0);
+  } else if (warp == 3 && lane == 0) {
+    // ---------------- C mover: each updated chunk (-acc, staged by the
+    // epilogue) is added into C by a TMA reduce (f32 add at L2), so C is never
+    // loaded into the SM; a slot is handed back once its reduce has read it
     const int ntiles = total_tiles > first ? (total_tiles - first + stride - 1) / stride : 0;
-    auto chunk_coords = [&](int g, int& x, int& y) {
+    const int G = ntiles * CHUNKS;
+    for (int g = 0; g < G; ++g) {
+      const int slot = g % CSLOTS;
+      if (!mbar_wait(&cdone[slot], (g / CSLOTS) & 1, abort)) break;
       const int t = first + (g / CHUNKS) * stride;
-      x = cx0 + (t % tiles_n) * BN + (g % CHUNKS) * 32;
-      y = cy0 + (t / tiles_n) * BM;
-    };
-    int issued = 0, processed = 0;   // C chunk loads issued / consumed (leader)
-    if (leader) {
-      for (int g = 0; g < CSLOTS && g < ntiles * CHUNKS; ++g, ++issued) {
-        int x, y;
-        chunk_coords(g, x, y);
-        mbar_expect_tx(&cfull[g % CSLOTS], CHUNK_BYTES);
-        tma_load_2d(cring + (g % CSLOTS) * CHUNK_BYTES, &mapC, &cfull[g % CSLOTS], x, y);
+      tma_reduce_add_2d(&mapC, cring + slot * CHUNK_BYTES, cx0 + (t % tiles_n) * BN + (g % CHUNKS) * 32,
+                        cy0 + (t / tiles_n) * BM);
+      bulk_commit();
+      // every reduce but the newest has read its slot
+      if (g >= 1) {
+        bulk_wait_read1();
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&cfree[(g - 1) % CSLOTS])) : "memory");
       }
     }
+    bulk_wait0();
+  } else if (warp >= 4) {
+    // ---------------- epilogue: 128 threads, thread = accumulator row; each
+    // chunk: TMEM -> registers, -acc (scaled) into a free slot, handed to the
+    // C mover for its reduce into C
+    const int q = warp - 4, r = q * 32 + lane;
+    const int ntiles = total_tiles > first ? (total_tiles - first + stride - 1) / stride : 0;
     for (int lt = 0; lt < ntiles; ++lt) {
       const int acc = lt & 1;
-      if (!epi_bar_and(mbar_wait(&tfull[acc], (lt >> 1) & 1, abort))) break;
+      if (!mbar_wait(&tfull[acc], (lt >> 1) & 1, abort)) break;
       tc_fence_after();
       bool ok = true;
       const int tile = first + lt * stride;
       const int tm0 = (tile / tiles_n) * BM, tn0 = (tile % tiles_n) * BN;
-      const float rs = F16 ? __ldg(invA + tm0 + r) : 1.f;
+      const float rs = F16 ? -__ldg(invA + tm0 + r) : -1.f;
       for (int c = 0; c < CHUNKS; ++c) {
         const int g = lt * CHUNKS + c, slot = g % CSLOTS;
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c * 32), v);
+        if (c == CHUNKS - 1) {
+          // every TMEM read of this accumulator is done
+          tc_fence_before();
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
+        }
         if constexpr (F16) {
           const float* cs = invB + ((tn0 + c * 32) >> 1);
 #pragma unroll
@@ -240,48 +245,20 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
             v[2 * j] *= f;
             v[2 * j + 1] *= f;
           }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = -v[j];
         }
-        if (!epi_bar_and(mbar_wait(&cfull[slot], (g / CSLOTS) & 1, abort))) { ok = false; break; }
+        if (g >= CSLOTS && !mbar_wait(&cfree[slot], ((g / CSLOTS) - 1) & 1, abort)) { ok = false; break; }
         unsigned char* rowp = cring + slot * CHUNK_BYTES + r * 128;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          float4* p = reinterpret_cast<float4*>(rowp + ((j ^ (r & 7)) << 4));
-          float4 cv = *p;
-          cv.x -= v[4 * j];
-          cv.y -= v[4 * j + 1];
-          cv.z -= v[4 * j + 2];
-          cv.w -= v[4 * j + 3];
-          *p = cv;
-        }
+        for (int j = 0; j < 8; ++j)
+          *reinterpret_cast<float4*>(rowp + ((j ^ (r & 7)) << 4)) =
+              make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         fence_async_smem();
-        epi_bar();
-        if (leader) {
-          int x, y;
-          chunk_coords(g, x, y);
-          tma_store_2d(&mapC, cring + slot * CHUNK_BYTES, x, y);
-          bulk_commit();
-          processed = g + 1;
-          // refill the previous chunk's slot: its store (all but the newest
-          // bulk group) has read its data, while this chunk's store stays in flight
-          const int gn = g - 1 + CSLOTS;
-          if (g >= 1 && gn < ntiles * CHUNKS) {
-            bulk_wait_read1();
-            chunk_coords(gn, x, y);
-            const int ps = gn % CSLOTS;
-            mbar_expect_tx(&cfull[ps], CHUNK_BYTES);
-            tma_load_2d(cring + ps * CHUNK_BYTES, &mapC, &cfull[ps], x, y);
-            issued = gn + 1;
-          }
-        }
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&cdone[slot])) : "memory");
       }
-      tc_fence_before();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
       if (!ok) break;
-    }
-    if (leader) {
-      bulk_wait0();
-      // (abort path) prefetched chunks that were never consumed land before exit
-      for (int g = processed; g < issued; ++g) mbar_wait_plain(&cfull[g % CSLOTS], (g / CSLOTS) & 1);
     }
   }
   tc_fence_before();
@@ -529,10 +506,10 @@ static int tc_num_sms() { return device_sm_count(); }
 static void tc_init_attrs() {
   static OncePerDevice once;
   once([] {
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::smem_bytes<2, 4>());
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::smem_bytes<2, 4>());
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<3, 2>());
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<3, 2>());
   });
 }
 
@@ -587,9 +564,9 @@ int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, in
       plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB, \
       status)
   if (plan.mode == MGT_TC_F16X2)
-    MGT_TC_LAUNCH(true, 2, 4);
+    MGT_TC_LAUNCH(true, 3, 2);
   else
-    MGT_TC_LAUNCH(false, 2, 4);
+    MGT_TC_LAUNCH(false, 3, 2);
 #undef MGT_TC_LAUNCH
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }

@@ -299,6 +299,16 @@ struct RefineWs {
     size_t off = 0;
     auto take = [&](size_t bytes) { char* p = b ? b + off : nullptr; off += (bytes + 255) & ~size_t(255); return p; };
     tc = residual_tc_supported(n, n, r);
+    rowexp = nullptr;
+    digits = nullptr;
+    if (tc) {
+      // M's row exponents and digits first: their place does not depend on
+      // nrhs, so a workspace prepared once serves solves of fewer columns
+      rowexp = (int*)take(n * sizeof(int));
+      off = (off + 1023) & ~size_t(1023);
+      digits = (unsigned char*)take(residual_tc_digits_bytes(n, n));
+      off = (off + 1023) & ~size_t(1023);
+    }
     Rr = (double2*)take(n * r * sizeof(double2));
     R32 = (float2*)take(n * r * sizeof(float2));
     D32 = (float2*)take(n * r * sizeof(float2));
@@ -307,14 +317,9 @@ struct RefineWs {
     Xs = nullptr;
     part = nullptr;
     part_elems = 0;
-    rowexp = nullptr;
-    digits = nullptr;
     tcw = nullptr;
     tcw_bytes = 0;
     if (tc) {
-      rowexp = (int*)take(n * sizeof(int));
-      off = (off + 1023) & ~size_t(1023);
-      digits = (unsigned char*)take(residual_tc_digits_bytes(n, n));
       off = (off + 1023) & ~size_t(1023);
       tcw_bytes = residual_tc_apply_bytes(n, n, r);
       tcw = take(tcw_bytes);
@@ -326,7 +331,8 @@ struct RefineWs {
     total = off;
   }
   // Rr = B - M X; prepared: the row exponents and digits of this M are in
-  // the workspace already (made by an earlier residual of the same solve)
+  // the workspace already (an earlier residual of the same solve, or
+  // mgt_refine_prepare); M may then be null
   int residual(const float4* M, int64_t ldm, const double2* X, int64_t ldx, const double2* B, int64_t ldb, int n,
                int nr, bool prepared, cudaStream_t s) {
     if (tc) {
@@ -416,10 +422,11 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
                                  int64_t n, const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
                                  double tol, int max_iter, void* work, size_t work_bytes, int* iters,
                                  double* rel_res, void* stream) {
-  if (!M || !LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || ldm < n || ldlu < n || ldb < nrhs ||
+  if (!LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || (M && ldm < n) || ldlu < n || ldb < nrhs ||
       ldx < nrhs || max_iter < 0)
     return MGT_ERR_ARG;
   RefineWs w(work, n, nrhs);
+  if (!M && !w.tc) return MGT_ERR_ARG;   // prepared digits exist only for the tensor-core residual
   if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
@@ -443,7 +450,7 @@ extern "C" int mgt_solve_refined(const void* M, int64_t ldm, const void* LU, int
   int it = 0;
   int dev_status = MGT_OK;
   for (;; ++it) {
-    e = w.residual((const float4*)M, ldm, Xd, ldx, Bd, ldb, nn, nr, it > 0, s);
+    e = w.residual((const float4*)M, ldm, Xd, ldx, Bd, ldb, nn, nr, it > 0 || !M, s);
     if (e != MGT_OK) return e;
     if (cudaMemsetAsync(w.norms + 1, 0, sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
     count_launch();
@@ -498,6 +505,15 @@ extern "C" int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
 
+extern "C" int mgt_refine_prepare(const void* M, int64_t ldm, int64_t n, int64_t nrhs, void* work, size_t work_bytes,
+                                  void* stream) {
+  if (!M || !work || n <= 0 || nrhs <= 0 || ldm < n) return MGT_ERR_ARG;
+  RefineWs w(work, n, nrhs);
+  if (!w.tc) return MGT_ERR_UNSUPPORTED;
+  if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
+  return residual_tc_prepare((const float4*)M, ldm, (int)n, (int)n, w.rowexp, w.digits, (cudaStream_t)stream);
+}
+
 // ---------------------------------------------------------------- stream-ordered refinement steps
 //
 // The same refinement as mgt_solve_refined, split into steps that only
@@ -528,15 +544,16 @@ extern "C" int mgt_refine_start(const void* LU, int64_t ldlu, const int32_t* per
 extern "C" int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, int64_t ldlu, const int32_t* perm,
                                   int64_t n, const void* B, int64_t ldb, void* X, int64_t ldx, int64_t nrhs,
                                   void* work, size_t work_bytes, void* stream) {
-  if (!M || !LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || ldm < n || ldlu < n || ldb < nrhs ||
+  if (!LU || !perm || !B || !X || !work || n <= 0 || nrhs <= 0 || (M && ldm < n) || ldlu < n || ldb < nrhs ||
       ldx < nrhs)
     return MGT_ERR_ARG;
   RefineWs w(work, n, nrhs);
+  if (!M && !w.tc) return MGT_ERR_ARG;
   if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const unsigned eg = (unsigned)((n * nrhs + 255) / 256);
-  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, false, s);
+  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, !M, s);
   if (e != MGT_OK) return e;
   count_launch();
   c128_to_c64_kernel<<<eg, 256, 0, s>>>(w.Rr, nr, w.R32, nr, nn, nr);
@@ -551,14 +568,15 @@ extern "C" int mgt_refine_correct(const void* M, int64_t ldm, const void* LU, in
 extern "C" int mgt_refine_norms(const void* M, int64_t ldm, int64_t n, const void* B, int64_t ldb, const void* X,
                                 int64_t ldx, int64_t nrhs, void* work, size_t work_bytes, double* norms_dev,
                                 void* stream) {
-  if (!M || !B || !X || !work || !norms_dev || n <= 0 || nrhs <= 0 || ldm < n || ldb < nrhs || ldx < nrhs)
+  if (!B || !X || !work || !norms_dev || n <= 0 || nrhs <= 0 || (M && ldm < n) || ldb < nrhs || ldx < nrhs)
     return MGT_ERR_ARG;
   RefineWs w(work, n, nrhs);
+  if (!M && !w.tc) return MGT_ERR_ARG;
   if (work_bytes < w.total) return MGT_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   const int nn = (int)n, nr = (int)nrhs;
   const int64_t tot = n * nrhs;
-  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, false, s);
+  int e = w.residual((const float4*)M, ldm, (const double2*)X, ldx, (const double2*)B, ldb, nn, nr, !M, s);
   if (e != MGT_OK) return e;
   if (cudaMemsetAsync(norms_dev, 0, 2 * sizeof(double), s) != cudaSuccess) return MGT_ERR_CUDA;
   count_launch(2);

@@ -201,9 +201,39 @@ def lu_solve(f, B):
     return X
 
 
-def solve_refined(Mdf, f, B, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER, require=True):
-    """Refined solve of M X = B (B complex128 n x R) with complex64 factors f
-    and the double-float matrix Mdf.  Returns (X, iterations, rel_residual)."""
+class RefineContext:
+    """The refinement's hold on M: its digits (the tensor-core residual's
+    operand, 14 B per entry) made once by mgt_refine_prepare in a refinement
+    workspace for up to max_nrhs columns, after which the double-float copy
+    may be freed.  Where the tensor-core residual is unavailable it keeps the
+    double-float matrix instead."""
+
+    def __init__(self, Mdf, max_nrhs=64):
+        lib = L.load()
+        self.n = Mdf.shape[0]
+        self.max_nrhs = int(max_nrhs)
+        nb = ctypes.c_size_t()
+        L.check(lib.mgt_refine_workspace_bytes(self.n, self.max_nrhs, ctypes.byref(nb)), "mgt_refine_workspace_bytes")
+        self.work = workspace(nb.value, Mdf.device)
+        st = lib.mgt_refine_prepare(_ptr(Mdf), self.n, self.n, self.max_nrhs, _ptr(self.work), self.work.numel(),
+                                    _stream())
+        if st == L.MGT_ERR_UNSUPPORTED:
+            self.Mdf, self.work = Mdf, None
+        else:
+            L.check(st, "mgt_refine_prepare")
+            self.Mdf = None
+
+
+def solve_refined(M, f, B, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER, require=True):
+    """Refined solve of M X = B (B complex128 n x R) with complex64 factors f.
+    M: the double-float matrix, or a RefineContext (right-hand sides wider
+    than it was prepared for are solved in blocks of columns).  Returns
+    (X, iterations, rel_residual)."""
+    if isinstance(M, RefineContext):
+        if M.work is None:
+            return solve_refined(M.Mdf, f, B, tol, max_iter, require)
+        return _solve_prepared(M, f, B, tol, max_iter, require)
+    Mdf = M
     lib = L.load()
     n = f.n
     B = B.contiguous()
@@ -221,6 +251,33 @@ def solve_refined(Mdf, f, B, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER, require
         return X, it.value, rr.value
     L.check(st, f"mgt_solve_refined (iterations {it.value}, relative residual {rr.value:.3e})")
     return X, it.value, rr.value
+
+
+def _solve_prepared(ctx, f, B, tol, max_iter, require):
+    lib = L.load()
+    n = f.n
+    B = B.contiguous()
+    R = B.shape[1]
+    X = torch.empty_like(B)
+    its, sq = [], 0.0
+    for c0 in range(0, R, ctx.max_nrhs):
+        Bc = B[:, c0:c0 + ctx.max_nrhs].contiguous()
+        Xc = torch.empty_like(Bc)
+        rc = Bc.shape[1]
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        st = lib.mgt_solve_refined(None, n, _ptr(f.lu), f.lu.stride(0), _ptr(f.perm), n, _ptr(Bc), rc, _ptr(Xc), rc,
+                                   rc, float(tol), int(max_iter), _ptr(ctx.work), ctx.work.numel(), ctypes.byref(it),
+                                   ctypes.byref(rr), _stream())
+        if not (st == L.MGT_ERR_NOT_CONVERGED and not require):
+            L.check(st, f"mgt_solve_refined (iterations {it.value}, relative residual {rr.value:.3e})")
+        X[:, c0:c0 + rc] = Xc
+        its.append(it.value)
+        if rc == R:
+            return X, it.value, rr.value
+        sq += (rr.value * torch.linalg.norm(Bc).item()) ** 2
+    nb = torch.linalg.norm(B).item()
+    return X, max(its), (sq ** 0.5 / nb if nb > 0 else sq ** 0.5)
 
 
 def residual(Mdf, X, B):
@@ -279,7 +336,10 @@ def solve_system(kind, points, k0, coef, shift, E0, precision="fp64", tol=DEFAUL
         return X
     if precision == "mixed":
         Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
-        f, X, it, rr = mixed_factor_solve(Mdf, M32, E0, _fresh(kind, points, k0, coef, shift), tol, max_iter)
+        # the digits replace the double-float copy before the LU needs its memory
+        ctx = RefineContext(Mdf, E0.shape[1])
+        del Mdf
+        f, X, it, rr = mixed_factor_solve(ctx, M32, E0, _fresh(kind, points, k0, coef, shift), tol, max_iter)
         if stats is not None:
             stats.update(method="mixed", iterations=it, rel_residual=rr, pivoting=f.pivoting)
         return X
@@ -300,9 +360,10 @@ def mixed_factor(M32, fresh_m32):
 
 def mixed_factor_solve(Mdf, M32, B, fresh_m32, tol=DEFAULT_TOL, max_iter=DEFAULT_MAX_ITER):
     """Factor M32 (tile pivoting first) and refine M X = B against the
-    double-float Mdf; if the refinement does not reach tol on tile-pivoted
-    factors, factor a fresh copy with partial pivoting and refine again.
-    Returns (factors, X, iterations, relative residual)."""
+    double-float Mdf (or a RefineContext made from it); if the refinement
+    does not reach tol on tile-pivoted factors, factor a fresh copy with
+    partial pivoting and refine again.  Returns (factors, X, iterations,
+    relative residual)."""
     f = mixed_factor(M32, fresh_m32)
     X, it, rr = solve_refined(Mdf, f, B, tol, max_iter, require=f.pivoting == "partial")
     if rr <= tol:
@@ -328,7 +389,10 @@ class SystemFactorization:
             self.Mdf = None
             self.f = lu_factor(M)
         elif precision == "mixed":
-            self.Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
+            Mdf, M32 = assemble_system(kind, points, k0, coef, shift, ("cdf", "c64"))
+            self.ctx = RefineContext(Mdf, 64)
+            self.Mdf = self.ctx.Mdf
+            del Mdf
             self._fresh = _fresh(kind, points, k0, coef, shift)
             self.f = mixed_factor(M32, self._fresh)
         else:
@@ -340,11 +404,11 @@ class SystemFactorization:
         if self.precision == "fp64":
             return lu_solve(self.f, B.to(torch.complex128))
         B = B.to(torch.complex128)
-        X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter, require=self.f.pivoting == "partial")
+        X, it, rr = solve_refined(self.ctx, self.f, B, self.tol, self.max_iter, require=self.f.pivoting == "partial")
         if rr > self.tol:
             # tile-pivoted factors that refinement cannot use: partial pivoting from here on
             self.f = lu_factor(self._fresh(), pivoting="partial")
-            X, it, rr = solve_refined(self.Mdf, self.f, B, self.tol, self.max_iter)
+            X, it, rr = solve_refined(self.ctx, self.f, B, self.tol, self.max_iter)
         self.last_iterations, self.last_residual = it, rr
         return X
 

@@ -204,6 +204,8 @@ class Server:
             raise RuntimeError("magreete_gb300.Server needs a CUDA GPU")
         self.device = torch.device("cuda", torch.cuda.current_device())
         free, _ = torch.cuda.mem_get_info(self.device)
+        # memory the caching allocator holds but no tensor uses is free for requests too
+        free += torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
         self.admission = Admission(self.budget)
         self.precision = precision

@@ -77,6 +77,7 @@ def test_invalid_arguments_rejected_before_any_device_work():
     assert lib.mgt_solve_refined(null, 100, null, 100, null, 100, null, 4, null, 4, 4, 1e-10, 10, null, 0,
                                  None, None, null) == ARG
     assert lib.mgt_refine_start(null, 100, null, 100, null, 4, null, 4, 4, null, 0, null) == ARG
+    assert lib.mgt_refine_prepare(null, 100, 100, 4, null, 0, null) == ARG
     assert lib.mgt_refine_correct(null, 100, null, 100, null, 100, null, 4, null, 4, 4, null, 0, null) == ARG
     assert lib.mgt_refine_norms(null, 100, 100, null, 4, null, 4, 4, null, 0, null, null) == ARG
     assert lib.mgt_column_dots(null, 4, null, 4, 100, 4, null, null) == ARG

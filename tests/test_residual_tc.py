@@ -116,3 +116,31 @@ def test_prepared_operator_matches_one_shot_residual():
         assert torch.equal(op(X, B), E.residual(Mdf, X, B))
     with pytest.raises(ValueError):
         op(X[:, :1].repeat(1, 41), B[:, :1].repeat(1, 41))
+
+
+def test_refinement_from_prepared_digits():
+    """mgt_refine_prepare, then the double-float matrix freed: refined solves
+    through the prepared digits give the same fields as solves from the
+    matrix (bitwise for one block of columns; wider right-hand sides in
+    column blocks within 1e-9)."""
+    from magreete_gb300 import engine as E
+    from magreete_gb300 import selfterm, serve
+    from magreete_gb300 import workloads as W
+    prob = W.disk_problem(1500, 31, 14.0, n_angles=40)
+    pts = prob.points.cuda()
+    shift = selfterm.diagonal_shift(prob.kind, prob.k0, prob.alpha, prob.radius)
+    coef = prob.alpha * prob.k0 ** 2
+    Mdf, M32 = E.assemble_system(prob.kind, pts, prob.k0, coef, shift, ("cdf", "c64"))
+    E0s, _ = serve.incident_fields(prob, pts, prob.detectors.cuda())
+    B = E0s.reshape(prob.n, -1).contiguous()
+    f = E.lu_factor(M32.clone(), pivoting="partial")
+    X_ref, it_ref, rr_ref = E.solve_refined(Mdf, f, B)
+    ctx = E.RefineContext(Mdf.clone(), B.shape[1])
+    X1, it1, rr1 = E.solve_refined(ctx, f, B)
+    # the norms are sums in atomic order: equal to rounding
+    assert torch.equal(X1, X_ref) and it1 == it_ref and rr1 == pytest.approx(rr_ref, rel=1e-12)
+    narrow = E.RefineContext(Mdf, 16)
+    del Mdf
+    X2, it2, rr2 = E.solve_refined(narrow, f, B)
+    assert rr2 <= 1e-10
+    assert (torch.linalg.norm(X2 - X_ref) / torch.linalg.norm(X_ref)).item() < 1e-9
