@@ -905,18 +905,19 @@ static std::atomic<int> g_fused_right{1};        // tensor-core LU: one fused pa
 // panel) U12 = L11^-1 A12 by forward substitution with the unit lower L11.
 template <typename T, int NB>
 __global__ void __launch_bounds__(256)
-lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int left_end, int right_begin,
-                    int right_end, PanelWs ws, int do_trsm) {
+lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, int left_begin, int left_end,
+                    int right_begin, int right_end, PanelWs ws, int do_trsm, const cplx<T>* __restrict__ Linv) {
   using V = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* buf = reinterpret_cast<V*>(smem_raw);   // [2*NB][kSwapCols]
   V* L = buf + 2 * NB * kSwapCols;            // [NB][NB]
   const int tid = threadIdx.x;
-  // columns [0, left_end) left of the panel, [right_begin, right_end) right of it
-  const int nleft_blocks = (left_end + kSwapCols - 1) / kSwapCols;
+  // columns [left_begin, left_end) left of the panel, [right_begin, right_end) right of it
+  const int nleft_blocks = max(0, left_end - left_begin + kSwapCols - 1) / kSwapCols;
   const bool right_cols = (int)blockIdx.x >= nleft_blocks;
   const bool right = right_cols && do_trsm;   // columns right of the panel that get the solve
-  const int col0 = right_cols ? right_begin + ((int)blockIdx.x - nleft_blocks) * kSwapCols : blockIdx.x * kSwapCols;
+  const int col0 = right_cols ? right_begin + ((int)blockIdx.x - nleft_blocks) * kSwapCols
+                              : left_begin + (int)blockIdx.x * kSwapCols;
   const int colend = right_cols ? right_end : left_end;
   const int ncols = min(kSwapCols, colend - col0);
   const int m = n - j0;
@@ -932,15 +933,34 @@ lu_swap_trsm_kernel(cplx<T>* __restrict__ A, int64_t lda, int n, int j0, int w, 
       cp_async_elem<(int)sizeof(V)>(buf + q * kSwapCols + cc, A + (int64_t)(j0 + sl.y) * lda + col0 + cc, true);
   }
   if (right) {
+    // L11 from the factor, or (tile pivoting) its inverse from the tile kernel
     for (int idx = tid; idx < w * w; idx += blockDim.x) {
       int i = idx / w, k = idx - i * w;
-      cp_async_elem<(int)sizeof(V)>(L + i * NB + k, A + (int64_t)(j0 + i) * lda + j0 + k, true);
+      cp_async_elem<(int)sizeof(V)>(L + i * NB + k, Linv ? Linv + i * NB + k : A + (int64_t)(j0 + i) * lda + j0 + k,
+                                    true);
     }
   }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  if (right) {
+  if (right && Linv) {
+    // U12 = L11^-1 X: thread = (column cc, rows i0 + 8 m), products independent
+    // across threads (no chain over the rows)
+    const int cc = tid & 31, i0 = tid >> 5;
+    V acc[NB / 8];
+#pragma unroll
+    for (int m = 0; m < NB / 8; ++m) acc[m] = czero<V>();
+    for (int k = 0; k < w; ++k) {
+      const V xk = buf[k * kSwapCols + cc];
+#pragma unroll
+      for (int m = 0; m < NB / 8; ++m) cfma(acc[m], L[(i0 + 8 * m) * NB + k], xk);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < NB / 8; ++m)
+      if (i0 + 8 * m < w && cc < kSwapCols) buf[(i0 + 8 * m) * kSwapCols + cc] = acc[m];
+    __syncthreads();
+  } else if (right) {
     // 8 lanes per column: lane = col_local * 8 + t8, 4 columns per warp
     const int warp = tid >> 5, lane = tid & 31;
     const int cc = warp * 4 + (lane >> 3), t8 = lane & 7;
@@ -1272,6 +1292,72 @@ constexpr int kTileLD = 65;   // padded row stride of the tile in shared memory
 constexpr int kCandLD = 128;  // a staged candidate row: columns 4 (j + k) + g < 128
 constexpr size_t kTileSmem = (2 * 64 * kTileLD + 2 * 32 * 33 + 2 * 8 * kCandLD) * sizeof(float2);
 
+// One level of the recursion, blocks of h = 2^LH rows: the (up to 8) items of
+// a thread are interleaved inside the k loop, so their dependent chains of
+// multiply-adds overlap (item = (block q, row i, column j), upper items first)
+template <int LH>
+__device__ __forceinline__ void tile_inv_level(float2* T, float2* S1, float2* S2, int tid) {
+  constexpr int h = 1 << LH, per = h * h, tot = 32 * h, M = (2 * tot + 255) / 256;
+  int qi[M], ii[M], jj[M];
+  bool val[M], up[M];
+  float2 acc[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int e = tid + 256 * m;
+    val[m] = e < 2 * tot;
+    up[m] = e < tot;
+    const int f = up[m] ? e : e - tot;
+    qi[m] = f >> (2 * LH);
+    ii[m] = (f >> LH) & (h - 1);
+    jj[m] = f & (h - 1);
+  }
+  // step 1: S1 = A^-1 B (upper), S2 = B A^-1 (lower; A^-1 unit lower, diagonal 1)
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int b = 2 * h * qi[m];
+    acc[m] = (val[m] && !up[m]) ? T[(b + h + ii[m]) * kTileLD + b + jj[m]] : make_float2(0.f, 0.f);
+  }
+#pragma unroll 4
+  for (int k = 0; k < h; ++k) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const int b = 2 * h * qi[m];
+      if (val[m] && up[m] && k >= ii[m])
+        cfma(acc[m], T[(b + ii[m]) * kTileLD + b + k], T[(b + k) * kTileLD + b + h + jj[m]]);
+      if (val[m] && !up[m] && k > jj[m])
+        cfma(acc[m], T[(b + h + ii[m]) * kTileLD + b + k], T[(b + k) * kTileLD + b + jj[m]]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+    if (val[m]) (up[m] ? S1 : S2)[qi[m] * per + ii[m] * h + jj[m]] = acc[m];
+  __syncthreads();
+  // step 2: B <- -(S1 C^-1) (upper), B <- -(C^-1 S2) (lower)
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+    acc[m] = (val[m] && !up[m]) ? S2[qi[m] * per + ii[m] * h + jj[m]] : make_float2(0.f, 0.f);
+#pragma unroll 4
+  for (int k = 0; k < h; ++k) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const int b = 2 * h * qi[m];
+      if (val[m] && up[m] && k <= jj[m])
+        cfma(acc[m], S1[qi[m] * per + ii[m] * h + k], T[(b + h + k) * kTileLD + b + h + jj[m]]);
+      if (val[m] && !up[m] && k < ii[m])
+        cfma(acc[m], T[(b + h + ii[m]) * kTileLD + b + h + k], S2[qi[m] * per + k * h + jj[m]]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    if (!val[m]) continue;
+    const int b = 2 * h * qi[m];
+    const float2 v = make_float2(-acc[m].x, -acc[m].y);
+    if (up[m]) T[(b + ii[m]) * kTileLD + b + h + jj[m]] = v;
+    else T[(b + h + ii[m]) * kTileLD + b + jj[m]] = v;
+  }
+  __syncthreads();
+}
+
 // In-place inverses of the upper triangle U (diagonal included) and of the
 // unit lower triangle L (strict lower part) of the 64 x 64 tile T, by block
 // recursion: for a block [[A, B], [0, C]] of U, the off-diagonal block of the
@@ -1285,40 +1371,12 @@ __device__ void tile_triangular_inverses(float2* T, float2* S1, float2* S2, int 
     T[i * kTileLD + i] = (u.x != 0.f || u.y != 0.f) ? crecip(u) : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  for (int h = 1; h < 64; h *= 2) {
-    const int nblk = 32 / h, per = h * h, tot = nblk * per;
-    // step 1: S1 = A^-1 B (upper), S2 = B A^-1 (lower); block q at rows / columns b = 2 h q
-    for (int e = tid; e < 2 * tot; e += 256) {
-      const bool up = e < tot;
-      const int f = up ? e : e - tot, q = f / per, i = (f % per) / h, j = f % h, b = 2 * h * q;
-      if (up) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (int k = i; k < h; ++k) cfma(acc, T[(b + i) * kTileLD + b + k], T[(b + k) * kTileLD + b + h + j]);
-        S1[q * per + i * h + j] = acc;
-      } else {
-        // B: rows b + h .., columns b ..; A^-1 unit lower, (A^-1)[k][j] for k > j, diagonal 1
-        float2 acc = T[(b + h + i) * kTileLD + b + j];
-        for (int k = j + 1; k < h; ++k) cfma(acc, T[(b + h + i) * kTileLD + b + k], T[(b + k) * kTileLD + b + j]);
-        S2[q * per + i * h + j] = acc;
-      }
-    }
-    __syncthreads();
-    // step 2: B <- -(S1 C^-1) (upper), B <- -(C^-1 S2) (lower)
-    for (int e = tid; e < 2 * tot; e += 256) {
-      const bool up = e < tot;
-      const int f = up ? e : e - tot, q = f / per, i = (f % per) / h, j = f % h, b = 2 * h * q;
-      if (up) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (int k = 0; k <= j; ++k) cfma(acc, S1[q * per + i * h + k], T[(b + h + k) * kTileLD + b + h + j]);
-        T[(b + i) * kTileLD + b + h + j] = make_float2(-acc.x, -acc.y);
-      } else {
-        float2 acc = S2[q * per + i * h + j];
-        for (int k = 0; k < i; ++k) cfma(acc, T[(b + h + i) * kTileLD + b + h + k], S2[q * per + k * h + j]);
-        T[(b + h + i) * kTileLD + b + j] = make_float2(-acc.x, -acc.y);
-      }
-    }
-    __syncthreads();
-  }
+  tile_inv_level<0>(T, S1, S2, tid);
+  tile_inv_level<1>(T, S1, S2, tid);
+  tile_inv_level<2>(T, S1, S2, tid);
+  tile_inv_level<3>(T, S1, S2, tid);
+  tile_inv_level<4>(T, S1, S2, tid);
+  tile_inv_level<5>(T, S1, S2, tid);
 }
 
 // One CTA of 256 threads; thread (r, g) = (tid / 4, tid % 4) holds the
@@ -1333,7 +1391,7 @@ __device__ void tile_triangular_inverses(float2* T, float2* S1, float2* S2, int 
 // position c, which gives the interchange slots directly.  Then all warps
 // invert U11 and L11 in place, for the rows below (L21 = A21 U11^-1) and the
 // columns to the right (U12 = L11^-1 A12).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 1)
 lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __restrict__ perm, PanelWs ws,
                float2* __restrict__ Uinv, float2* __restrict__ Linv) {
   // A: the tile's top-left element (row j0, column j0); w <= 64
@@ -1345,6 +1403,7 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
   float2* cand = S2 + 32 * 33;                          // [2][8][kCandLD]: each warp's best row, by column parity
   __shared__ uint32_t s_key[2][8];
   __shared__ int s_row[2][8];
+  __shared__ float2 s_inv[2][8];                       // 1 / each warp's candidate pivot
   __shared__ int s_piv[64];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r = tid >> 2, g = tid & 3;
@@ -1362,7 +1421,9 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
   for (int k = 0; k < 16; ++k) a[k] = T[r * kTileLD + 4 * k + g];
   bool active = r < w;
   for (int j = 0; j < 16 && 4 * j < w; ++j) {
-#pragma unroll
+    // not unrolled: u only selects threads, and one copy of the column body
+    // keeps the loop within the instruction cache
+#pragma unroll 1
     for (int u = 0; u < 4; ++u) {
       const int c = 4 * j + u;
       if (c >= w) break;
@@ -1375,32 +1436,34 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
       if (mx != 0u && (lane >> 2) == (int)(ml >> 2)) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) cb[warp * kCandLD + 4 * (j + k) + g] = a[k];
+        // the candidate's reciprocal before the barrier, off the chain after it
+        if (g == u) {
+          const bool z = a[0].x == 0.f && a[0].y == 0.f;
+          s_inv[buf][warp] = z ? make_float2(0.f, 0.f) : crecip(a[0]);
+        }
       }
       if (lane == 0) {
         s_key[buf][warp] = mx;
         s_row[buf][warp] = warp * 8 + (int)(ml >> 2);
       }
       __syncthreads();
-      int best = 0;
-      uint32_t bk = s_key[buf][0];
-#pragma unroll
-      for (int q = 1; q < 8; ++q) {
-        const uint32_t kq = s_key[buf][q];
-        if (kq > bk) { bk = kq; best = q; }
-      }
+      // the winning warp: largest bid, lowest warp (lowest rows) on ties; lanes
+      // 0..7 read one bid each and two warp reductions decide
+      const uint32_t kq = lane < 8 ? s_key[buf][lane] : 0u;
+      const uint32_t kmax = __reduce_max_sync(0xffffffffu, kq);
+      const int best = (int)__reduce_min_sync(0xffffffffu, (lane < 8 && kq == kmax) ? (uint32_t)lane : 8u);
       const int p = s_row[buf][best];
       const float2* prow = cb + best * kCandLD;
-      const float2 piv = prow[c];
-      if (tid < 64 && tid >= c) F[c * kTileLD + tid] = prow[tid];
+      const float2 pinv = s_inv[buf][best];
       if (r == p) {
         if (g == 0) {
           s_piv[c] = r;
+          const float2 piv = prow[c];
           if (piv.x == 0.f && piv.y == 0.f && ws.status[1] == 0) ws.status[1] = j0 + c + 1;
         }
         active = false;
       }
-      const bool nz = piv.x != 0.f || piv.y != 0.f;
-      float2 l = (g == u && nz) ? cmul(a[0], crecip(piv)) : make_float2(0.f, 0.f);
+      float2 l = g == u ? cmul(a[0], pinv) : make_float2(0.f, 0.f);
       l.x = __shfl_sync(0xffffffffu, l.x, (lane & ~3) | u);
       l.y = __shfl_sync(0xffffffffu, l.y, (lane & ~3) | u);
       if (active) {
@@ -1408,6 +1471,8 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
 #pragma unroll
         for (int k = 0; k < 16; ++k) cfms(a[k], l, prow[4 * (j + k) + g]);
       }
+      // row c of U (read from the staged row until the next column's barrier)
+      if (tid < 64 && tid >= c) F[c * kTileLD + tid] = prow[tid];
     }
 #pragma unroll
     for (int k = 0; k < 15; ++k) a[k] = a[k + 1];
@@ -1449,6 +1514,96 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
     const bool inw = i < w && k < w;
     Uinv[idx] = (inw && k >= i) ? v : make_float2(0.f, 0.f);
     Linv[idx] = (inw && k < i) ? v : make_float2(i == k ? 1.f : 0.f, 0.f);
+  }
+}
+
+// Rows below the first tile of a 128-wide block (tile pivoting), fused:
+// L21 = A21 U11^-1 on the first panel's w columns, then the second panel's wb
+// columns A22 -= L21 U12 (U12: the first panel's rows of those columns,
+// already solved).  32 rows per CTA, thread = (row, every eighth column).
+__global__ void __launch_bounds__(256)
+lu_l21_update_kernel(float2* __restrict__ A, int64_t lda, int rows, int w, int wb, const float2* __restrict__ Uinv,
+                     const float2* __restrict__ U12) {
+  // A: first row below the tile, first column of the panel; U12: the panel's
+  // first row, first column of the second panel
+  extern __shared__ __align__(16) unsigned char fused_smem[];
+  float2* Ui = reinterpret_cast<float2*>(fused_smem);   // [64][64]
+  float2* Us = Ui + 64 * 64;                             // [64][64] U12
+  float2* Ar = Us + 64 * 64;                             // [32][64] A21, then L21
+  float2* Cr = Ar + 32 * 64;                             // [32][64] A22
+  const int tid = threadIdx.x, r0 = blockIdx.x * 32;
+  for (int idx = tid; idx < 64 * 32; idx += 256) cp_async_elem<16>(Ui + 2 * idx, Uinv + 2 * idx, true);
+  for (int idx = tid; idx < 64 * 64; idx += 256) {
+    const int k = idx >> 6, c = idx & 63;
+    const bool in = k < w && c < wb;
+    cp_async_elem<8>(Us + idx, in ? U12 + (int64_t)k * lda + c : U12, in);
+  }
+  for (int idx = tid; idx < 32 * 64; idx += 256) {
+    const int r = idx >> 6, k = idx & 63;
+    const bool ra = r0 + r < rows && k < w, rc = r0 + r < rows && k < wb;
+    cp_async_elem<8>(Ar + idx, ra ? A + (int64_t)(r0 + r) * lda + k : A, ra);
+    cp_async_elem<8>(Cr + idx, rc ? A + (int64_t)(r0 + r) * lda + w + k : A, rc);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int r = tid >> 3, g = tid & 7;
+  float2 acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = make_float2(0.f, 0.f);
+  for (int i = 0; i < w; ++i) {
+    const float2 a = Ar[r * 64 + i];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cfma(acc[q], a, Ui[i * 64 + g + 8 * q]);
+  }
+  __syncthreads();   // every thread has read its row of A21
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int k = g + 8 * q;
+    Ar[r * 64 + k] = acc[q];
+    if (r0 + r < rows && k < w) A[(int64_t)(r0 + r) * lda + k] = acc[q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = Cr[r * 64 + g + 8 * q];
+  for (int k = 0; k < w; ++k) {
+    const float2 l = Ar[r * 64 + k];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cfms(acc[q], l, Us[k * 64 + g + 8 * q]);
+  }
+  if (r0 + r < rows) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int c = g + 8 * q;
+      if (c < wb) A[(int64_t)(r0 + r) * lda + w + c] = acc[q];
+    }
+  }
+}
+constexpr size_t kL21UpdateSmem = (2 * 64 * 64 + 2 * 32 * 64) * sizeof(float2);
+
+// The interchanges of tile t (rows 64 t .., position q holds tile row
+// perm[64 t + q] - 64 t: rows move only within their tile) on the columns
+// left of the tile's outer block, which the panels left alone.  Block
+// (32 columns, tile): gather the tile's rows through shared memory, write
+// them back in order.
+__global__ void __launch_bounds__(256)
+lu_tile_left_perm_kernel(float2* __restrict__ A, int64_t lda, int n, const int32_t* __restrict__ perm, int outer) {
+  __shared__ float2 buf[64][33];
+  const int j0 = blockIdx.y * 64, w = min(64, n - j0);
+  const int jb = j0 / outer * outer, c0 = blockIdx.x * 32;
+  if (c0 >= jb) return;
+  const int ncols = min(32, jb - c0);
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < w * 32; idx += 256) {
+    const int q = idx >> 5, cc = idx & 31;
+    const int src = perm[j0 + q] - j0;
+    if (cc < ncols && src >= 0 && src < w) buf[q][cc] = A[(int64_t)(j0 + src) * lda + c0 + cc];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < w * 32; idx += 256) {
+    const int q = idx >> 5, cc = idx & 31;
+    const int src = perm[j0 + q] - j0;
+    if (cc < ncols && src >= 0 && src < w && src != q) A[(int64_t)(j0 + q) * lda + c0 + cc] = buf[q][cc];
   }
 }
 
@@ -1558,6 +1713,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     cudaFuncSetAttribute(lu_panel_reg_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)reg_panel_smem(NB, sizeof(V)));
     cudaFuncSetAttribute(lu_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+    cudaFuncSetAttribute(lu_l21_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kL21UpdateSmem);
   });
   PanelWs ws = panel_ws(work);
   if (cudaMemsetAsync(work, 0, 32, s) != cudaSuccess) return MGT_ERR_CUDA;   // status, nslot
@@ -1574,7 +1730,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     return std::min(G, gmax > 0 ? std::min(gmax, sms) : sms);
   };
   // factor columns [j0, j0+w) over rows [j0, n); the interchanges go to slot set `set`
-  auto panel_only = [&](int j0, int w, int set) -> int {
+  auto panel_only = [&](int j0, int w, int set, bool with_l21 = true) -> int {
     if constexpr (sizeof(T) == 4) {
       if (opt.pivoting == MGT_PIVOT_TILE) {
         LuWsLayout Lw;
@@ -1585,7 +1741,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
                                                   Ui, Li);
         count_launch();
         const int below = n - j0 - w;
-        if (below > 0) {
+        if (below > 0 && with_l21) {
           lu_l21_kernel<<<(below + 31) / 32, 256, 0, s>>>(A + (int64_t)(j0 + w) * lda + j0, lda, below, w, Ui);
           count_launch();
         }
@@ -1644,22 +1800,44 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     return MGT_OK;
   };
   // apply the interchanges of the panel at j0 (slot set `set`) to columns
-  // [0, left_end) and [right_begin, right_end); with do_trsm the latter also get
-  // U12 = L11^-1 A12 on the panel's rows
-  auto swap = [&](cudaStream_t st, int j0, int w, int set, int left_end, int right_begin, int right_end,
-                  int do_trsm) {
-    const int nleft = (left_end + kSwapCols - 1) / kSwapCols;
+  // [left_begin, left_end) and [right_begin, right_end); with do_trsm the
+  // latter also get U12 = L11^-1 A12 on the panel's rows
+  auto swap = [&](cudaStream_t st, int j0, int w, int set, int left_begin, int left_end, int right_begin,
+                  int right_end, int do_trsm) {
+    const int nleft = left_end > left_begin ? (left_end - left_begin + kSwapCols - 1) / kSwapCols : 0;
     const int nright = right_end > right_begin ? (right_end - right_begin + kSwapCols - 1) / kSwapCols : 0;
     if (nleft + nright > 0) {
-      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, st>>>(A, lda, n, j0, w, left_end, right_begin,
-                                                                    right_end, panel_ws(work, set), do_trsm);
+      // tile pivoting: the tile kernel left L11^-1 of this panel in slot `set`
+      const V* Linv = nullptr;
+      if (opt.pivoting == MGT_PIVOT_TILE && do_trsm)
+        Linv = reinterpret_cast<const V*>((char*)work + LuWsLayout().inv) + (size_t)set * kNBmax * kNBmax;
+      lu_swap_trsm_kernel<T, NB><<<nleft + nright, 256, sm2, st>>>(A, lda, n, j0, w, left_begin, left_end,
+                                                                    right_begin, right_end, panel_ws(work, set),
+                                                                    do_trsm, Linv);
       count_launch();
     }
+  };
+  // Tile pivoting moves rows only within their 64-row tile, and nothing reads
+  // a tile's L entries left of its outer block again before the end: those
+  // columns take the tile's interchanges in one pass at the end
+  // (lu_tile_left_perm_kernel) instead of once per panel.
+  const bool defer_left = opt.pivoting == MGT_PIVOT_TILE;
+  auto finish = [&](int outer) -> int {
+    if constexpr (sizeof(T) == 4) {
+      if (defer_left && n > NB) {
+        lu_tile_left_perm_kernel<<<dim3((n + kSwapCols - 1) / kSwapCols, (n + NB - 1) / NB), 256, 0, s>>>(
+            reinterpret_cast<float2*>(A), lda, n, perm, outer);
+        count_launch();
+      }
+    } else {
+      (void)outer;
+    }
+    return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
   };
   // one inner panel, then its interchanges on every other column
   auto panel_step = [&](int j0, int w, int do_trsm) -> int {
     int e = panel_only(j0, w, 0);
-    if (e == MGT_OK) swap(s, j0, w, 0, j0, j0 + w, n, do_trsm);
+    if (e == MGT_OK) swap(s, j0, w, 0, defer_left ? j0 : 0, j0, j0 + w, n, do_trsm);
     return e;
   };
   auto update_on = [&](cudaStream_t st, int r0, int c0, int k0, int K, int rows, int cols, bool dominant,
@@ -1690,7 +1868,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       if (e == MGT_OK) e = update(j0 + w, j0 + w, j0, w, n - j0 - w, n - j0 - w, true);
       if (e != MGT_OK) return e;
     }
-    return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+    return finish(NB);
   }
   // tensor-core path: 128-wide outer blocks made of two 64-wide inner panels,
   // so that the trailing update runs with K = 128 (half the C traffic per flop)
@@ -1719,14 +1897,30 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   // the second panel's columns brought up to date
   auto block_panels = [&](int J0, int far) -> int {
     const int W = std::min(2 * NB, n - J0), wa = std::min(NB, W), wb = W - wa, j1 = J0 + wa;
-    int e = panel_only(J0, wa, 0);
+    // tile pivoting: the rows below the first tile get L21 together with the
+    // second panel's update, once the swap kernel has solved U12
+    const bool fuse = defer_left && sizeof(T) == 4 && wb > 0;
+    int e = panel_only(J0, wa, 0, !fuse);
     if (e != MGT_OK) return e;
-    swap(s, J0, wa, 0, J0, j1, std::min(far, J0 + W), 1);
+    // (tile pivoting) columns left of J0 wait for the final pass; the
+    // second panel's rows of the first panel's columns (L_BA, read by the
+    // right-column pass) are swapped here
+    swap(s, J0, wa, 0, defer_left ? J0 : 0, J0, j1, std::min(far, J0 + W), 1);
     if (wb > 0) {
-      e = update(j1, j1, J0, wa, n - j1, wb, false);
+      if (fuse) {
+        if constexpr (sizeof(T) == 4) {
+          const float2* Ui = reinterpret_cast<const float2*>((char*)work + LuWsLayout().uinv);
+          lu_l21_update_kernel<<<(n - j1 + 31) / 32, 256, kL21UpdateSmem, s>>>(
+              reinterpret_cast<float2*>(A) + (int64_t)j1 * lda + J0, lda, n - j1, wa, wb, Ui,
+              reinterpret_cast<const float2*>(A) + (int64_t)J0 * lda + j1);
+          count_launch();
+        }
+      } else {
+        e = update(j1, j1, J0, wa, n - j1, wb, false);
+      }
       if (e == MGT_OK) e = panel_only(j1, wb, 1);
       if (e != MGT_OK) return e;
-      swap(s, j1, wb, 1, j1, 0, 0, 0);
+      swap(s, j1, wb, 1, defer_left ? J0 : 0, j1, 0, 0, 0);
     }
     return MGT_OK;
   };
@@ -1747,9 +1941,9 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
         return;
       }
     }
-    swap(s, J0, wa, 0, 0, J0 + W, n, 1);
+    swap(s, J0, wa, 0, 0, 0, J0 + W, n, 1);
     if (wb > 0) {
-      swap(s, j1, wb, 1, 0, J0 + W, n, 0);
+      swap(s, j1, wb, 1, 0, 0, J0 + W, n, 0);
       lu_preupdate_trsm_kernel<T, NB><<<(right + kSwapCols - 1) / kSwapCols, 256, sm3, s>>>(A, lda, n, J0, wa, j1,
                                                                                            wb, J0 + W);
       count_launch();
@@ -1819,7 +2013,7 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
     if (e != MGT_OK) return e;
     block_right(P0);
   }
-  return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
+  return finish(2 * NB);
 }
 
 // ---------------------------------------------------------------- solves
