@@ -1292,6 +1292,19 @@ constexpr int kTileLD = 65;   // padded row stride of the tile in shared memory
 constexpr int kCandLD = 128;  // a staged candidate row: columns 4 (j + k) + g < 128
 constexpr size_t kTileSmem = (2 * 64 * kTileLD + 2 * 32 * 33 + 2 * 8 * kCandLD) * sizeof(float2);
 
+// 1/z for the tile's pivots: Smith's scaling with two correctly rounded
+// reciprocals instead of three divisions (each result within a few ulp of
+// the quotient; the LU is only FP32-accurate and the mixed method's
+// refinement certifies the solution)
+__device__ __forceinline__ float2 crecip_tile(float2 z) {
+  if (fabsf(z.x) >= fabsf(z.y)) {
+    const float r = z.y * __frcp_rn(z.x), inv = __frcp_rn(fmaf(z.y, r, z.x));
+    return make_float2(inv, -r * inv);
+  }
+  const float r = z.x * __frcp_rn(z.y), inv = __frcp_rn(fmaf(z.x, r, z.y));
+  return make_float2(r * inv, -inv);
+}
+
 // One level of the recursion, blocks of h = 2^LH rows: the (up to 8) items of
 // a thread are interleaved inside the k loop, so their dependent chains of
 // multiply-adds overlap (item = (block q, row i, column j), upper items first)
@@ -1368,7 +1381,7 @@ __device__ __forceinline__ void tile_inv_level(float2* T, float2* S1, float2* S2
 __device__ void tile_triangular_inverses(float2* T, float2* S1, float2* S2, int tid) {
   for (int i = tid; i < 64; i += 256) {
     const float2 u = T[i * kTileLD + i];
-    T[i * kTileLD + i] = (u.x != 0.f || u.y != 0.f) ? crecip(u) : make_float2(0.f, 0.f);
+    T[i * kTileLD + i] = (u.x != 0.f || u.y != 0.f) ? crecip_tile(u) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   tile_inv_level<0>(T, S1, S2, tid);
@@ -1439,7 +1452,7 @@ lu_tile_kernel(float2* __restrict__ A, int64_t lda, int w, int j0, int32_t* __re
         // the candidate's reciprocal before the barrier, off the chain after it
         if (g == u) {
           const bool z = a[0].x == 0.f && a[0].y == 0.f;
-          s_inv[buf][warp] = z ? make_float2(0.f, 0.f) : crecip(a[0]);
+          s_inv[buf][warp] = z ? make_float2(0.f, 0.f) : crecip_tile(a[0]);
         }
       }
       if (lane == 0) {

@@ -281,16 +281,24 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kInvLd) * sizeof(V);
   const size_t smem = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
   const size_t smem_w = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
-  static int max_ctas = 0, max_ctas_w = 0;
+  // resident-CTA caps per device (set with the device's function attributes)
+  static int max_ctas_dev[kMaxDevices], max_ctas_w_dev[kMaxDevices];
   static OncePerDevice once;
-  once([smem, smem_w, smem_inv] {
+  const int dev = current_device();
+  once([smem, smem_w, smem_inv, dev] {
+    int& max_ctas = max_ctas_dev[dev];
+    int& max_ctas_w = max_ctas_w_dev[dev];
     cudaFuncSetAttribute(diag_inverse_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
     cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    max_ctas = resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTG>, smem);
+    // at most two CTAs per SM: the block row on the dependency chain shares its
+    // SM with fewer off-chain products (n = 12000, 64 RHS: 5.15 -> 4.80 ms per
+    // complex64 LU solve against the three that fit)
+    max_ctas = std::min(resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTG>, smem), 2 * device_sm_count());
     if constexpr (sizeof(T) == 4) {
       cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTGWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem_w);
-      max_ctas_w = resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTGWide>, smem_w);
+      max_ctas_w = std::min(resident_ctas((const void*)tri_solve_kernel<T, UPPER, kTGWide>, smem_w),
+                            2 * device_sm_count());
     }
   });
   // wide column groups where block rows alone give enough parallelism
@@ -309,14 +317,14 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   count_launch();
   if constexpr (sizeof(T) == 4) {
     if (wide) {
-      const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas_w);
+      const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_w_dev[dev]));
       tri_solve_kernel<T, UPPER, kTGWide><<<grid, 256, smem_w, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags,
                                                                      epoch, status);
       return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
     }
   }
   {
-    const int grid = (int)std::min<int64_t>((int64_t)nb * ng, max_ctas);
+    const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_dev[dev]));
     tri_solve_kernel<T, UPPER, kTG><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch,
                                                              status);
   }
