@@ -99,6 +99,57 @@ diag_inverse_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, cplx<T>* 
   for (int idx = tid; idx < kTB * kTB; idx += 256) out[idx] = Xs[(idx >> 6) * kInvLd + (idx & 63)];
 }
 
+// W_i = Inv_i F_(i, j): the inverted diagonal block times the factor block of
+// the last dependency j of block row i (j = i - 1 for L, i + 1 for U), so
+// that the solve can form Inv_i (B_i - all other products) before block j
+// is done and needs only X_i = Z - W_i X_j after it.  One CTA per block row,
+// thread = (4 rows, 4 columns) of W_i.
+template <typename T, bool UPPER>
+__global__ void __launch_bounds__(256)
+chain_factor_kernel(const cplx<T>* __restrict__ F, int64_t ldf, int n, const cplx<T>* __restrict__ Inv,
+                    cplx<T>* __restrict__ W) {
+  using V = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* Is = reinterpret_cast<V*>(smem_raw);   // [kTB][kTB + 1]
+  V* Fs = Is + kTB * (kTB + 1);              // [kTB][kTB + 1]
+  const int tid = threadIdx.x, i = blockIdx.x, nb = gridDim.x;
+  const int j = UPPER ? i + 1 : i - 1;
+  if (j < 0 || j >= nb) return;
+  const int r0 = i * kTB, rb = min(kTB, n - r0), c0 = j * kTB, cb = min(kTB, n - c0);
+  const V* inv = Inv + (int64_t)i * kTB * kTB;
+  for (int idx = tid; idx < kTB * kTB; idx += 256) {
+    const int r = idx >> 6, c = idx & 63;
+    cp_async_elem<(int)sizeof(V)>(Is + r * (kTB + 1) + c, inv + idx, true);
+    const bool ok = r < rb && c < cb;
+    cp_async_elem<(int)sizeof(V)>(Fs + r * (kTB + 1) + c, ok ? F + (int64_t)(r0 + r) * ldf + c0 + c : F, ok);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int tr = tid >> 4, tc = tid & 15;   // rows 4 tr .., columns tc + 16 q
+  V acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[a][q] = czero<V>();
+  for (int k = 0; k < kTB; ++k) {
+    V f[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) f[q] = Fs[k * (kTB + 1) + tc + 16 * q];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const V x = Is[(4 * tr + a) * (kTB + 1) + k];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cfma(acc[a][q], x, f[q]);
+    }
+  }
+  V* out = W + (int64_t)i * kTB * kTB;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[(4 * tr + a) * kTB + tc + 16 * q] = acc[a][q];
+}
+
 // acc (64 x TG, a TR x TC tile per thread: rows TR tr + i, columns tc + TPR j)
 // -= A (64 x 64, smem, padded) * Y (64 x TG, smem)
 template <int TG, typename V>
@@ -120,12 +171,18 @@ __device__ __forceinline__ void block_gemm_sub(V (&acc)[TriTile<TG>::TR][TriTile
 }
 
 // Stage st of work item (block row i, ndep dependencies) into buf: for
-// st < ndep the factor block of dependency st (it does not depend on the
-// flag), for st == ndep the inverted diagonal block (full 64 x 64).
+// st < ndep - 1 the factor block of dependency st (it does not depend on the
+// flag), then the inverted diagonal block (full 64 x 64; the only stage when
+// ndep = 0), then W_i = Inv_i F_(i, last dependency).
 template <bool UPPER, typename V>
 __device__ __forceinline__ void tri_stage(V* buf, int st, int ndep, const V* __restrict__ F, int64_t ldf,
-                                          const V* __restrict__ Inv, int i, int nb, int n, int r0, int rb, int tid) {
-  if (st < ndep) {
+                                          const V* __restrict__ Inv, const V* __restrict__ W, int i, int nb, int n,
+                                          int r0, int rb, int tid) {
+  if (ndep > 0 && st == ndep) {
+    const V* w = W + (int64_t)i * kTB * kTB;
+    for (int idx = tid; idx < kTB * kTB; idx += 256)
+      cp_async_elem<(int)sizeof(V)>(buf + (idx >> 6) * (kTB + 1) + (idx & 63), w + idx, true);
+  } else if (st < ndep - 1) {
     const int j = UPPER ? nb - 1 - st : st;
     const int c0 = j * kTB, cb = min(kTB, n - c0);
     for (int idx = tid; idx < kTB * kTB; idx += 256) {
@@ -149,8 +206,8 @@ __device__ __forceinline__ void tri_stage(V* buf, int st, int ndep, const V* __r
 template <typename T, bool UPPER, int TG>
 __global__ void __launch_bounds__(256)
 tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
-                 cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols, unsigned* counter, unsigned* flags,
-                 const unsigned* epoch_ptr, int* status) {
+                 const cplx<T>* __restrict__ W, cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols,
+                 unsigned* counter, unsigned* flags, const unsigned* epoch_ptr, int* status) {
   // flag value of this solve: bumped on the device before the launch, so a
   // replay from a CUDA graph never sees the previous run's flags as ready
   const unsigned epoch = *(volatile const unsigned*)epoch_ptr;
@@ -183,12 +240,15 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
         const int r = TR * tr + a, c = cg + tc + TPR * b;
         acc[a][b] = (r < rb && c < ncols) ? X[(int64_t)(r0 + r) * ldx + c] : czero<V>();
       }
-    // dependencies in completion order: ascending for L, descending for U
+    // dependencies in completion order: ascending for L, descending for U.
+    // All but the last are applied as they complete; then Z = Inv_i acc is
+    // formed before the last one is done, and after it X_i = Z - W_i X_last:
+    // one product on the chain from block to block instead of two.
     const int ndep = UPPER ? nb - 1 - i : i;
-    tri_stage<UPPER>(Asb, 0, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
-    for (int d = 0; d < ndep; ++d) {
-      const V* As = Asb + (NBUF == 2 ? (d & 1) * kAs : 0);
-      if (NBUF == 2) tri_stage<UPPER>(Asb + ((d + 1) & 1) * kAs, d + 1, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
+    auto stage = [&](V* buf, int st) { tri_stage<UPPER>(buf, st, ndep, F, ldf, Inv, W, i, nb, n, r0, rb, tid); };
+    auto bufof = [&](int st) { return Asb + (NBUF == 2 ? (st & 1) * kAs : 0); };
+    // wait for dependency d's completion flag and stage its rows of X in Ys
+    auto take_dep = [&](int d) -> bool {
       const int j = UPPER ? nb - 1 - d : d;
       const int c0 = j * kTB, cb = min(kTB, n - c0);
       if (tid == 0) {
@@ -198,24 +258,35 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
           if (it > 64) __nanosleep(32);
         }
       }
-      if (NBUF == 2) cp_async_wait<1>(); else cp_async_wait<0>();
       __syncthreads();
-      if (s_fail) {
-        cp_async_wait<0>();
-        return;
-      }
+      if (s_fail) return false;
       for (int idx = tid; idx < kTB * TG; idx += 256) {
         int r = idx / TG, c = idx % TG;
         Ys[idx] = (r < cb && cg + c < ncols) ? ldcg(X + (int64_t)(c0 + r) * ldx + cg + c) : czero<V>();
       }
       __syncthreads();
-      block_gemm_sub<TG>(acc, As, Ys, tr, tc);
+      return true;
+    };
+    stage(bufof(0), 0);
+    for (int d = 0; d < ndep - 1; ++d) {
+      if (NBUF == 2) stage(bufof(d + 1), d + 1);
+      if (NBUF == 2) cp_async_wait<1>(); else cp_async_wait<0>();
+      if (!take_dep(d)) {
+        cp_async_wait<0>();
+        return;
+      }
+      block_gemm_sub<TG>(acc, bufof(d), Ys, tr, tc);
       __syncthreads();
-      if (NBUF == 1) tri_stage<UPPER>(Asb, d + 1, ndep, F, ldf, Inv, i, nb, n, r0, rb, tid);
+      if (NBUF == 1) stage(bufof(d + 1), d + 1);
     }
-    // X_i = Inv_i * acc, Inv_i in the last stage's buffer
-    const V* As = Asb + (NBUF == 2 ? (ndep & 1) * kAs : 0);
-    cp_async_wait<0>();
+    // Z = Inv_i * acc (Inv_i is stage max(ndep - 1, 0)); W_i loads meanwhile
+    const int sinv = ndep > 0 ? ndep - 1 : 0;
+    if (NBUF == 2 && ndep > 0) {
+      stage(bufof(ndep), ndep);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
 #pragma unroll
     for (int a = 0; a < TR; ++a)
 #pragma unroll
@@ -226,18 +297,27 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
     for (int a = 0; a < TR; ++a)
 #pragma unroll
       for (int b = 0; b < TC; ++b) out[a][b] = czero<V>();
-    block_gemm_sub<TG>(out, As, Ys, tr, tc);   // out = -Inv * acc
+    block_gemm_sub<TG>(out, bufof(sinv), Ys, tr, tc);   // out = -Z
+#pragma unroll
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TC; ++b) {
+        out[a][b].x = -out[a][b].x;
+        out[a][b].y = -out[a][b].y;
+      }
+    __syncthreads();
+    if (ndep > 0) {
+      if (NBUF == 1) stage(bufof(ndep), ndep);
+      cp_async_wait<0>();
+      if (!take_dep(ndep - 1)) return;
+      block_gemm_sub<TG>(out, bufof(ndep), Ys, tr, tc);   // X_i = Z - W_i X_last
+    }
 #pragma unroll
     for (int a = 0; a < TR; ++a)
 #pragma unroll
       for (int b = 0; b < TC; ++b) {
         const int r = TR * tr + a, c = cg + tc + TPR * b;
-        if (r < rb && c < ncols) {
-          V v = out[a][b];
-          v.x = -v.x;
-          v.y = -v.y;
-          X[(int64_t)(r0 + r) * ldx + c] = v;
-        }
+        if (r < rb && c < ncols) X[(int64_t)(r0 + r) * ldx + c] = out[a][b];
       }
     __threadfence();
     __syncthreads();
@@ -258,7 +338,8 @@ __global__ void tri_start_kernel(unsigned* counter, unsigned* mark, unsigned* fl
   for (int f = i; f < nflags; f += gridDim.x * blockDim.x) flags[f] = 0;
 }
 
-// counter + status (256 B), flags (groups x blocks), inverted diagonal blocks (L and U)
+// counter + status (256 B), flags (groups x blocks), inverted diagonal blocks
+// (L and U) and the chain factors W (L and U)
 size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem) {
   const int64_t nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG;
   size_t flags = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
@@ -281,14 +362,16 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   const size_t smem_inv = (size_t)(kTB * (kTB + 1) + kTB * kInvLd) * sizeof(V);
   const size_t smem = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTG) * sizeof(V);
   const size_t smem_w = (size_t)(tri_nbuf<T>() * kTB * (kTB + 1) + kTB * kTGWide) * sizeof(V);
+  const size_t smem_cf = (size_t)(2 * kTB * (kTB + 1)) * sizeof(V);
   // resident-CTA caps per device (set with the device's function attributes)
   static int max_ctas_dev[kMaxDevices], max_ctas_w_dev[kMaxDevices];
   static OncePerDevice once;
   const int dev = current_device();
-  once([smem, smem_w, smem_inv, dev] {
+  once([smem, smem_w, smem_inv, smem_cf, dev] {
     int& max_ctas = max_ctas_dev[dev];
     int& max_ctas_w = max_ctas_w_dev[dev];
     cudaFuncSetAttribute(diag_inverse_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
+    cudaFuncSetAttribute(chain_factor_kernel<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cf);
     cudaFuncSetAttribute(tri_solve_kernel<T, UPPER, kTG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // at most two CTAs per SM: the block row on the dependency chain shares its
     // SM with fewer off-chain products (n = 12000, 64 RHS: 5.15 -> 4.80 ms per
@@ -308,9 +391,12 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   unsigned* counter = (unsigned*)work;
   unsigned* flags = (unsigned*)((char*)work + 256);
   size_t flag_bytes = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
+  // inverted diagonal blocks (L, then U), then the chain factors W (L, then U)
   V* inv = (V*)((char*)work + 256 + flag_bytes) + (UPPER ? (size_t)nb * kTB * kTB : 0);
-  count_launch();
+  V* wch = (V*)((char*)work + 256 + flag_bytes) + 2 * (size_t)nb * kTB * kTB + (UPPER ? (size_t)nb * kTB * kTB : 0);
+  count_launch(2);
   diag_inverse_kernel<T, UPPER><<<nb, 256, smem_inv, s>>>(F, ldf, n, inv);
+  chain_factor_kernel<T, UPPER><<<nb, 256, smem_cf, s>>>(F, ldf, n, inv, wch);
   unsigned* epoch = counter + 1;   // completion mark, set by tri_start_kernel
   count_launch();
   tri_start_kernel<<<std::max(1, std::min(nb * ng, 1 << 16) / 256 + 1), 256, 0, s>>>(counter, epoch, flags, nb * ng);
@@ -318,15 +404,15 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   if constexpr (sizeof(T) == 4) {
     if (wide) {
       const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_w_dev[dev]));
-      tri_solve_kernel<T, UPPER, kTGWide><<<grid, 256, smem_w, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags,
-                                                                     epoch, status);
+      tri_solve_kernel<T, UPPER, kTGWide><<<grid, 256, smem_w, s>>>(F, ldf, inv, wch, X, ldx, n, nrhs, counter,
+                                                                     flags, epoch, status);
       return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
     }
   }
   {
     const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_dev[dev]));
-    tri_solve_kernel<T, UPPER, kTG><<<grid, 256, smem, s>>>(F, ldf, inv, X, ldx, n, nrhs, counter, flags, epoch,
-                                                             status);
+    tri_solve_kernel<T, UPPER, kTG><<<grid, 256, smem, s>>>(F, ldf, inv, wch, X, ldx, n, nrhs, counter, flags,
+                                                             epoch, status);
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
