@@ -182,7 +182,7 @@ int mgt_lu_solve(int dtype, const void* LU, int64_t n, int64_t lda, const int32_
  * MGT_C128: FP64 SIMT.  MGT_C64 with use_tensor_cores = 0: FP32 SIMT;
  * use_tensor_cores = 1: tcgen05 tensor cores with hi/lo split operands
  * (FP32-level accuracy; the scheme is MGT_TUNE_TC_PRECISION: F16x2 with
- * kind::f16 by default, or TF32x3 with kind::tf32), K <= 128, ldc even;
+ * kind::f16 by default, or TF32x3 with kind::tf32), K <= 256, ldc even;
  * needs mgt_cgemm_workspace_bytes(max(M, N)) bytes of workspace.
  */
 int mgt_cgemm_workspace_bytes(int64_t nmax, size_t* bytes);
@@ -341,6 +341,11 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
  *   MGT_TUNE_SYM_ASSEMBLY 1 (default): mgt_assemble_system evaluates each pair
  *                        of points once and writes both mirror-image blocks
  *                        (bitwise the same matrix); 0: every block evaluated
+ *   MGT_TUNE_WIDE_UPDATE smallest trailing order at which the complex64
+ *                        tensor-core LU with tile pivoting pairs two 128-wide
+ *                        blocks, so that the columns right of the pair take
+ *                        one trailing update with K = 256 (default 8192;
+ *                        0: never)
  * Set by the batched sweep and its autotuner; mgt_get_tuning returns the value.
  */
 #define MGT_TUNE_PANEL_ROWS 1
@@ -353,6 +358,7 @@ int mgt_column_dots(const void* A, int64_t lda, const void* B, int64_t ldb, int6
 #define MGT_TUNE_FUSED_RIGHT 8
 #define MGT_TUNE_PANEL_CLUSTER 9
 #define MGT_TUNE_SYM_ASSEMBLY 10
+#define MGT_TUNE_WIDE_UPDATE 11
 #define MGT_TC_TF32X3 0
 #define MGT_TC_F16X2 1
 int mgt_set_tuning(int key, int value);

@@ -32,6 +32,7 @@ MGT_TUNE_LOOKAHEAD = 7
 MGT_TUNE_FUSED_RIGHT = 8
 MGT_TUNE_PANEL_CLUSTER = 9
 MGT_TUNE_SYM_ASSEMBLY = 10
+MGT_TUNE_WIDE_UPDATE = 11
 MGT_TC_TF32X3, MGT_TC_F16X2 = 0, 1
 MGT_PIVOT_PARTIAL, MGT_PIVOT_TILE = 0, 1
 

@@ -1,5 +1,5 @@
 // Tensor-core (tcgen05) complex trailing update for the complex64 LU:
-//   C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 128.
+//   C (M x N, complex64) -= A (M x K) * B (K x N),  K <= 256.
 // Two split-product schemes: F16x2 with kind::f16 MMAs (the default) and
 // TF32x3 with kind::tf32 MMAs (MGT_TUNE_TC_PRECISION).
 //
@@ -24,16 +24,18 @@
 // (column's) largest flush to zero, an absolute error below that of FP32
 // rounding of the row's largest entry.
 //
-// Kernel: persistent, one CTA per SM walking 128 x 128 tiles of C' (128 rows,
-// 64 complex columns):
+// Kernel: persistent, one CTA per SM walking 128 x 256 tiles of C' (128 rows,
+// 128 complex columns; N = 256 keeps the MMA's shared-memory operand reads
+// and the operand bytes per flop below those of a square 128 x 128 tile):
 //   warp 0 lane 0 : TMA producer (cp.async.bulk.tensor, 128B swizzle) of the
-//                   A_hi/A_lo (128 rows) and B_hi/B_lo (128 rows of B'^T)
+//                   A_hi/A_lo (128 rows) and B_hi/B_lo (256 rows of B'^T)
 //                   tiles of each K block (one 128-byte row: 64 fp16 or 32
-//                   fp32), 3-stage mbarrier ring
-//   warp 1 lane 0 : tcgen05.mma issuer (M = 128, N = 128, 32 bytes of K per
+//                   fp32), 2-stage mbarrier ring of 96 KB stages
+//   warp 1 lane 0 : tcgen05.mma issuer (M = 128, N = 256, 32 bytes of K per
 //                   instruction, 12 instructions per K block), tcgen05.commit
 //                   to free a stage and, at the end, to publish the accumulator
-//   warp 2        : TMEM allocation / deallocation (2 accumulators x 128 columns)
+//   warp 2        : TMEM allocation / deallocation (2 accumulators x 256
+//                   columns: all of TMEM)
 //   warp 3 lane 0 : C mover: TMA reduce-adds of 128 x 32 chunks into C
 //   warps 4-7     : epilogue: tcgen05.ld 32 columns at a time, -acc staged
 // Every wait is bounded; on expiry the CTA records MGT_ERR_TIMEOUT, drains
@@ -57,16 +59,17 @@ namespace mgt {
 namespace tc {
 
 constexpr int BM = 128;            // tile rows (M)
-constexpr int BN = 128;            // tile real columns (N') = 64 complex columns
-constexpr int KR = 256;            // real K stride of the split buffers (2 * 128 complex)
+constexpr int BN = 256;            // tile real columns (N') = 128 complex columns
+constexpr int KMAX = 256;          // largest complex K of one update
+constexpr int KR = 2 * KMAX;       // real K stride of the split buffers
 constexpr uint32_t A_TILE = BM * 128;      // 16 KB: 128 rows of one 128-byte swizzle row
-constexpr uint32_t B_TILE = BN * 128;      // 16 KB
-constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 64 KB
+constexpr uint32_t B_TILE = BN * 128;      // 32 KB
+constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;   // 96 KB
 constexpr int CHUNKS = BN / 32;            // epilogue chunks per tile (32 fp32 columns each)
 constexpr uint32_t CHUNK_BYTES = BM * 128; // 16 KB
 constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int THREADS = 256;
-// pipeline shape: operand stages x C ring slots (3 x 2: 192 + 32 KB)
+// pipeline shape: operand stages x C ring slots (2 x 2: 192 + 32 KB)
 template <int STAGES, int CSLOTS>
 constexpr size_t smem_bytes() {
   return STAGES * STAGE_BYTES + CSLOTS * CHUNK_BYTES + 1024 /* alignment slack */ + 256;
@@ -105,13 +108,15 @@ __device__ __forceinline__ void mma_split(uint32_t d_tmem, uint64_t a, uint64_t 
 // with a TMA reduce (f32 add at L2), handing a slot back once its reduce has
 // read it.
 // invA / invB (F16 mode): inverse row scales of A and inverse complex-column
-// scales of B, relative to the block being updated.
+// scales of B.  The update reads the B split from row boff (twice its first
+// complex column) on, so that one split serves several launches.
 template <bool F16, int STAGES, int CSLOTS>
 __global__ void __launch_bounds__(THREADS, 1)
 cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                     const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
-                    const __grid_constant__ CUtensorMap mapC, int cx0, int cy0, int tiles_n, int total_tiles,
-                    int kblocks, const float* __restrict__ invA, const float* __restrict__ invB, int* status) {
+                    const __grid_constant__ CUtensorMap mapC, int cx0, int cy0, int boff, int tiles_n,
+                    int total_tiles, int kblocks, const float* __restrict__ invA, const float* __restrict__ invB,
+                    int* status) {
   constexpr int BK = Mode<F16>::BK;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -159,8 +164,8 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
         mbar_expect_tx(&full[s], STAGE_BYTES);
         tma_load_2d(st, &mapAhi, &full[s], kb * BK, m0);
         tma_load_2d(st + A_TILE, &mapAlo, &full[s], kb * BK, m0);
-        tma_load_2d(st + 2 * A_TILE, &mapBhi, &full[s], kb * BK, n0);
-        tma_load_2d(st + 2 * A_TILE + B_TILE, &mapBlo, &full[s], kb * BK, n0);
+        tma_load_2d(st + 2 * A_TILE, &mapBhi, &full[s], kb * BK, boff + n0);
+        tma_load_2d(st + 2 * A_TILE + B_TILE, &mapBlo, &full[s], kb * BK, boff + n0);
       }
     }
     // (abort path) the last stages' loads land before the CTA may exit
@@ -238,7 +243,7 @@ cgemm_split3_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_con
           asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
         }
         if constexpr (F16) {
-          const float* cs = invB + ((tn0 + c * 32) >> 1);
+          const float* cs = invB + ((boff + tn0 + c * 32) >> 1);
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const float f = rs * __ldg(cs + j);
@@ -298,21 +303,24 @@ __global__ void split_a_kernel(const float2* __restrict__ A, int64_t lda, int M,
   Alo[o] = v - h;
 }
 
-// Columns N .. (grid end) are written as zeros so that the tile columns past
-// the matrix edge accumulate exactly zero (TMA stores clip the inner
-// dimension only at 16-byte granularity; a zero update leaves those bytes as
-// they were loaded).
+// B splits: one CTA per SB_COLS complex columns of B, all K rows staged in
+// shared memory.  Columns N .. (grid end) are written as zeros so that the
+// tile columns past the matrix edge accumulate exactly zero (TMA stores clip
+// the inner dimension only at 16-byte granularity; a zero update leaves those
+// bytes as they were loaded).
+constexpr int SB_COLS = 16;
+
 __global__ void split_b_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, int kcols,
                                float* __restrict__ Bhi, float* __restrict__ Blo) {
-  __shared__ float2 t[128][33];
-  const int j0 = blockIdx.x * 32;
-  for (int idx = threadIdx.x; idx < 128 * 32; idx += blockDim.x) {
-    int k = idx / 32, jj = idx - k * 32;
+  __shared__ float2 t[KMAX][SB_COLS + 1];
+  const int j0 = blockIdx.x * SB_COLS, krows = kcols >> 1;
+  for (int idx = threadIdx.x; idx < krows * SB_COLS; idx += blockDim.x) {
+    int k = idx / SB_COLS, jj = idx - k * SB_COLS;
     t[k][jj] = (k < K && j0 + jj < N) ? B[(int64_t)k * ldb + j0 + jj] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  // 64 output rows (2 per column j) x kcols reals
-  for (int idx = threadIdx.x; idx < 64 * kcols; idx += blockDim.x) {
+  // 2 SB_COLS output rows (2 per column j) x kcols reals
+  for (int idx = threadIdx.x; idx < 2 * SB_COLS * kcols; idx += blockDim.x) {
     int r = idx / kcols, kr = idx - r * kcols;
     int jj = r >> 1, j = j0 + jj;
     int k = kr >> 1;
@@ -373,19 +381,19 @@ __global__ void split_a_f16_kernel(const float2* __restrict__ A, int64_t lda, in
 // Columns N .. (grid end) are zero (see split_b_kernel).
 __global__ void split_b_f16_kernel(const float2* __restrict__ B, int64_t ldb, int K, int N, int kcols,
                                    __half* __restrict__ Bhi, __half* __restrict__ Blo, float* __restrict__ invB) {
-  __shared__ float2 t[128][33];
-  __shared__ float sc[32];
-  const int j0 = blockIdx.x * 32;
-  for (int idx = threadIdx.x; idx < 128 * 32; idx += blockDim.x) {
-    int k = idx / 32, jj = idx - k * 32;
+  __shared__ float2 t[KMAX][SB_COLS + 1];
+  __shared__ float sc[SB_COLS];
+  const int j0 = blockIdx.x * SB_COLS, krows = kcols >> 1;
+  for (int idx = threadIdx.x; idx < krows * SB_COLS; idx += blockDim.x) {
+    int k = idx / SB_COLS, jj = idx - k * SB_COLS;
     t[k][jj] = (k < K && j0 + jj < N) ? B[(int64_t)k * ldb + j0 + jj] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   // column scales: warp w handles columns w, w + 8, ...
-  for (int jj = threadIdx.x >> 5; jj < 32; jj += blockDim.x >> 5) {
+  for (int jj = threadIdx.x >> 5; jj < SB_COLS; jj += blockDim.x >> 5) {
     const int lane = threadIdx.x & 31;
     unsigned mx = 0;
-    for (int k = lane; k < 128; k += 32)
+    for (int k = lane; k < krows; k += 32)
       mx = max(mx, max(__float_as_uint(fabsf(t[k][jj].x)), __float_as_uint(fabsf(t[k][jj].y))));
     mx = __reduce_max_sync(0xffffffffu, mx);
     int e = 0;
@@ -399,7 +407,7 @@ __global__ void split_b_f16_kernel(const float2* __restrict__ B, int64_t ldb, in
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 64 * kcols; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < 2 * SB_COLS * kcols; idx += blockDim.x) {
     int r = idx / kcols, kr = idx - r * kcols;
     int jj = r >> 1, j = j0 + jj;
     int k = kr >> 1;
@@ -506,10 +514,10 @@ static int tc_num_sms() { return device_sm_count(); }
 static void tc_init_attrs() {
   static OncePerDevice once;
   once([] {
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::smem_bytes<3, 2>());
-    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc::smem_bytes<3, 2>());
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<false, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<2, 2>());
+    cudaFuncSetAttribute(tc::cgemm_split3_kernel<true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc::smem_bytes<2, 2>());
   });
 }
 
@@ -520,7 +528,7 @@ static int tc_kcols(const TcPlan& plan, int K) {
 
 int tc_split_a(const TcPlan& plan, int M, int K, const float2* A, int64_t lda, cudaStream_t s) {
   if (M <= 0 || K <= 0) return MGT_OK;
-  if (K > 128 || M > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  if (K > tc::KMAX || M > plan.nmax) return MGT_ERR_UNSUPPORTED;
   const int kcols = tc_kcols(plan, K);
   count_launch();
   if (plan.mode == MGT_TC_F16X2) {
@@ -536,10 +544,10 @@ int tc_split_a(const TcPlan& plan, int M, int K, const float2* A, int64_t lda, c
 
 int tc_split_b(const TcPlan& plan, int N, int K, const float2* B, int64_t ldb, cudaStream_t s) {
   if (N <= 0 || K <= 0) return MGT_OK;
-  if (K > 128 || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  if (K > tc::KMAX || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
   const int kcols = tc_kcols(plan, K);
   // cover every column of the last tile (2N rounded up to BN reals)
-  const int bgrid = (int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + 31) / 32);
+  const int bgrid = (int)((((2 * (int64_t)N + tc::BN - 1) / tc::BN) * tc::BN / 2 + tc::SB_COLS - 1) / tc::SB_COLS);
   count_launch();
   if (plan.mode == MGT_TC_F16X2)
     tc::split_b_f16_kernel<<<bgrid, 256, 0, s>>>(B, ldb, K, N, kcols, (__half*)plan.Bhi, (__half*)plan.Blo,
@@ -550,9 +558,9 @@ int tc_split_b(const TcPlan& plan, int N, int K, const float2* B, int64_t ldb, c
 }
 
 int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, int cx0, int cy0, int* status,
-            cudaStream_t s, int max_ctas) {
+            cudaStream_t s, int max_ctas, int bcol) {
   if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
-  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  if (K > tc::KMAX || M > plan.nmax || bcol < 0 || (int64_t)bcol + N > plan.nmax) return MGT_ERR_UNSUPPORTED;
   tc_init_attrs();
   const int kblocks = tc_kcols(plan, K) / (plan.mode == MGT_TC_F16X2 ? tc::Mode<true>::BK : tc::Mode<false>::BK);
   const int tiles_n = (2 * N + tc::BN - 1) / tc::BN, tiles_m = (M + tc::BM - 1) / tc::BM;
@@ -561,12 +569,12 @@ int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, in
   count_launch();
 #define MGT_TC_LAUNCH(F16, ST, CS)                                                                              \
   tc::cgemm_split3_kernel<F16, ST, CS><<<ctas, tc::THREADS, tc::smem_bytes<ST, CS>(), s>>>(                    \
-      plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, tiles_n, total, kblocks, plan.invA, plan.invB, \
-      status)
+      plan.mAhi, plan.mAlo, plan.mBhi, plan.mBlo, cmap, cx0, cy0, 2 * bcol, tiles_n, total, kblocks, plan.invA,    \
+      plan.invB, status)
   if (plan.mode == MGT_TC_F16X2)
-    MGT_TC_LAUNCH(true, 3, 2);
+    MGT_TC_LAUNCH(true, 2, 2);
   else
-    MGT_TC_LAUNCH(false, 3, 2);
+    MGT_TC_LAUNCH(false, 2, 2);
 #undef MGT_TC_LAUNCH
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }
@@ -574,7 +582,7 @@ int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, in
 int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, const float2* A, int64_t lda,
                 const float2* B, int64_t ldb, int cx0, int cy0, int* status, cudaStream_t s, int max_ctas) {
   if (M <= 0 || N <= 0 || K <= 0) return MGT_OK;
-  if (K > 128 || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
+  if (K > tc::KMAX || M > plan.nmax || N > plan.nmax) return MGT_ERR_UNSUPPORTED;
   int e = tc_split_a(plan, M, K, A, lda, s);
   if (e == MGT_OK) e = tc_split_b(plan, N, K, B, ldb, s);
   if (e == MGT_OK) e = tc_gemm(plan, cmap, M, N, K, cx0, cy0, status, s, max_ctas);
@@ -603,7 +611,7 @@ extern "C" int mgt_cgemm_sub(int dtype, int use_tensor_cores, int64_t M, int64_t
   if (dtype != MGT_C64) return MGT_ERR_ARG;
   if (!use_tensor_cores)
     return gemm_sub<float>((int)M, (int)N, (int)K, (const float2*)A, lda, (const float2*)B, ldb, (float2*)C, ldc, s);
-  if (K > 128) return MGT_ERR_UNSUPPORTED;
+  if (K > tc::KMAX) return MGT_ERR_UNSUPPORTED;
   int64_t nmax = std::max(M, N);
   if (!work || work_bytes < tc_scratch_bytes(nmax) + 256) return MGT_ERR_WORKSPACE;
   if (!tc_available()) return MGT_ERR_UNSUPPORTED;

@@ -31,7 +31,7 @@ bool tc_available();
 // 16-byte aligned base) viewed as fp32 (rows x 2 cols), 128 x 32 boxes.
 int tc_make_cmap(CUtensorMap* map, float2* C, int64_t rows, int64_t cols, int64_t ldc);
 
-// C -= A (M x K) * B (K x N), K <= 128, where C is the M x N block of the
+// C -= A (M x K) * B (K x N), K <= 256, where C is the M x N block of the
 // matrix described by cmap starting at fp32 column cx0 (= 2 * complex
 // column) and row cy0; the block must extend to the matrix's last row and
 // column (TMA stores are clipped there).  max_ctas <= 0: one CTA per SM.
@@ -42,7 +42,8 @@ int gemm_sub_tc(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K
 // the tcgen05 kernel, which reads only the split buffers and the C block.
 int tc_split_a(const TcPlan& plan, int M, int K, const float2* A, int64_t lda, cudaStream_t s);
 int tc_split_b(const TcPlan& plan, int N, int K, const float2* B, int64_t ldb, cudaStream_t s);
+// bcol: the first column of B (within the split) this launch uses.
 int tc_gemm(const TcPlan& plan, const CUtensorMap& cmap, int M, int N, int K, int cx0, int cy0, int* status,
-            cudaStream_t s, int max_ctas = 0);
+            cudaStream_t s, int max_ctas = 0, int bcol = 0);
 
 }  // namespace mgt

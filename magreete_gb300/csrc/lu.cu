@@ -895,6 +895,9 @@ constexpr int kSwapCols = 32;
 // run-time tuning knobs (set by the autotuner; see mgt_set_tuning)
 static std::atomic<int> g_panel_rows{kPanelRowsTarget};
 static std::atomic<int> g_outer_block{128};
+// complex64 tensor-core LU with tile pivoting: pair 128-wide blocks (one
+// K = 256 trailing update for both) while the trailing order is at least this
+static std::atomic<int> g_wide_min{8192};
 static std::atomic<int> g_panel_max_ctas{0};     // 0: one per SM
 static std::atomic<int> g_cooperative{1};        // panel launched with the cooperative attribute
 static std::atomic<int> g_panel_reg{1};          // register-resident panel: 0 never, 1 complex64, 2 both
@@ -1244,6 +1247,7 @@ static std::atomic<int> g_panel_cluster{1};     // complex64 panels of <= 16 CTA
 struct LuOpts {
   int pivoting = MGT_PIVOT_PARTIAL;
   int panel_rows, outer_block, panel_max_ctas, cooperative, panel_reg, lookahead, fused_right, panel_cluster;
+  int wide_min;
   LuOpts() {
     panel_rows = g_panel_rows.load(std::memory_order_relaxed);
     outer_block = g_outer_block.load(std::memory_order_relaxed);
@@ -1253,6 +1257,7 @@ struct LuOpts {
     lookahead = g_lookahead.load(std::memory_order_relaxed);
     fused_right = g_fused_right.load(std::memory_order_relaxed);
     panel_cluster = g_panel_cluster.load(std::memory_order_relaxed);
+    wide_min = g_wide_min.load(std::memory_order_relaxed);
   }
 };
 
@@ -1895,11 +1900,12 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
   });
   // Lookahead (cooperative panels, not under stream capture): the trailing
   // update of block J0 first brings the next block's columns up to date, then
-  // the rest of it runs on a side stream with its CTAs capped to leave the
-  // next panels their SMs, while this stream factors the next block's two
-  // inner panels and applies their interchanges to the columns the side
-  // stream does not touch.  The far-right interchanges, the second panel's
-  // pre-update and the U12 solve follow once the side stream has finished.
+  // the rest of it runs on a side stream (its first columns with the CTAs
+  // capped to leave the next panels their SMs, the others on every SM), while
+  // this stream factors the next block's two inner panels and applies their
+  // interchanges to the columns the side stream does not touch.  The
+  // far-right interchanges, the second panel's pre-update and the U12 solve
+  // follow once the side stream has finished.
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(s, &cap);
   SideStream* side = nullptr;
@@ -1977,8 +1983,17 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       if (cudaEventRecord(side->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, side->fork, 0) != cudaSuccess)
         return MGT_ERR_CUDA;
       dom_begin(s2);
-      const int reserve = opt.pivoting == MGT_PIVOT_TILE ? 16 : panel_ctas(M);
-      e = tc_gemm(tc->plan, tc->cmap, M, rest, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - reserve));
+      // the first columns beside the next block's panels, on the SMs they
+      // leave free; the rest, by when the panels should be done, on every SM
+      // (a persistent launch keeps the SMs it started on)
+      const bool tile = opt.pivoting == MGT_PIVOT_TILE;
+      const int reserve = tile ? 16 : panel_ctas(M);
+      const double t_pan = tile ? 3e-4 : 2.0 * NB * 4.5e-6 + 1e-4;
+      const double head = t_pan * 3e14 * (sms - reserve) / sms / (8.0 * M * (double)W);
+      const int c1 = (int)std::min<double>(rest, (std::floor(head / (2 * NB)) + 1) * (2 * NB));
+      e = tc_gemm(tc->plan, tc->cmap, M, c1, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - reserve));
+      if (e == MGT_OK && c1 < rest)
+        e = tc_gemm(tc->plan, tc->cmap, M, rest - c1, W, 2 * (P0 + WN + c1), P0, ws.status, s2, 0, c1);
       dom_end(s2, 8.0 * M * (double)rest * W, sizeof(V) * (2.0 * M * (double)rest + (double)W * rest));
       // once forked, the join is recorded whatever happened
       const bool joined = cudaEventRecord(side->join, s2) == cudaSuccess;
@@ -1988,43 +2003,76 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       return MGT_ERR_UNSUPPORTED;
     }
   };
+  // Paired blocks (tile pivoting, while the trailing order is at least
+  // opt.wide_min): once block X at P0 is factored and its right-column
+  // pass done, X's update goes only to the next block Y's columns (every row
+  // below X) and to Y's rows of the columns right of Y; Y is factored, and
+  // the columns right of Y then take the update of both blocks as one
+  // product with K = 256 (half the C traffic per flop of two K = 128
+  // updates).  Tile pivoting moves Y's rows only within Y's tiles, every one
+  // of which already carries X's update.
+  auto pair_update = [&](int X0, int Y0, int WY) -> int {
+    if constexpr (sizeof(T) == 4) {
+      const int KX = Y0 - X0, M = n - Y0, far0 = Y0 + WY, nfar = n - far0;
+      const float2* L21 = reinterpret_cast<const float2*>(A + (int64_t)Y0 * lda + X0);
+      const float2* U12 = reinterpret_cast<const float2*>(A + (int64_t)X0 * lda + Y0);
+      dom_begin(s);
+      int e = tc_split_a(tc->plan, M, KX, L21, lda, s);
+      if (e == MGT_OK) e = tc_split_b(tc->plan, WY + nfar, KX, U12, lda, s);
+      if (e == MGT_OK) e = tc_gemm(tc->plan, tc->cmap, M, WY, KX, 2 * Y0, Y0, ws.status, s);
+      // Y's rows are the first WY rows of the split L21
+      if (e == MGT_OK && nfar > 0)
+        e = tc_gemm(tc->plan, tc->cmap, WY, nfar, KX, 2 * far0, Y0, ws.status, s, 0, WY);
+      const double cells = (double)M * WY + (double)WY * nfar;
+      dom_end(s, 8.0 * cells * KX, sizeof(V) * (2.0 * cells + (double)M * KX + (double)KX * (WY + nfar)));
+      return e;
+    } else {
+      (void)X0; (void)Y0; (void)WY;
+      return MGT_ERR_UNSUPPORTED;
+    }
+  };
   if constexpr (sizeof(T) != 4) side = nullptr;   // the tensor-core path is complex64 only
+  const bool pairs = sizeof(T) == 4 && opt.pivoting == MGT_PIVOT_TILE && opt.wide_min > 0;
   int e = block_panels(0, n);
   if (e != MGT_OK) return e;
   block_right(0);
-  for (int J0 = 0; J0 < n; J0 += 2 * NB) {
-    const int W = std::min(2 * NB, n - J0);
-    const int P0 = J0 + W;                       // next block
-    if (P0 >= n) break;
+  // the factored columns [K0, K0 + KW) (one block, or a pair) whose update of
+  // the trailing matrix is pending
+  int K0 = 0, KW = std::min(2 * NB, n);
+  while (K0 + KW < n) {
+    const int P0 = K0 + KW;                      // next block
     const int WN = std::min(2 * NB, n - P0);
     const int rest = n - P0 - WN;
-    // overlap only where it pays: the side update runs on the SMs the next
-    // panels leave free (estimates: update at ~250 TF/s on the full GPU, two
-    // inner panels at ~4.5 us per column plus their interchanges)
-    bool overlap = side != nullptr && rest > 0;
-    if (overlap) {
-      const bool tile = opt.pivoting == MGT_PIVOT_TILE;
-      const int G = tile ? 16 : panel_ctas(n - P0);
-      const double t_upd = 8.0 * (n - P0) * (double)rest * W / 2.5e14;
-      const double t_pan = tile ? 2 * 40e-6 + 1e-4 : 2.0 * NB * 4.5e-6 + 1e-4;
-      overlap = sms - G >= 16 && std::max(t_upd * sms / (sms - G), t_pan) < t_upd + t_pan;
-    }
+    // the side update takes the SMs the panels leave free only for about the
+    // panels' time (lookahead_update), so the overlap pays whenever there is
+    // a rest, unless partial-pivoting panels would leave it too few SMs
+    const bool overlap = side != nullptr && rest > 0 &&
+                         (opt.pivoting == MGT_PIVOT_TILE || sms - panel_ctas(n - P0) >= 16);
     if (!overlap) {
-      e = update(P0, P0, J0, W, n - P0, n - P0, true);
+      e = update(P0, P0, K0, KW, n - P0, n - P0, true);
       if (e == MGT_OK) e = block_panels(P0, n);
       if (e != MGT_OK) return e;
-      block_right(P0);
-      continue;
+    } else {
+      // A[P0:, P0:] -= L21 U12 of the pending columns: the operand splits (the
+      // rows of L21 are permuted by the next panels' interchanges) and the
+      // next block's columns here; the rest of the update on the side stream
+      e = lookahead_update(K0, KW, P0, WN, rest, side->s);
+      if (e == MGT_OK) e = block_panels(P0, P0 + WN);
+      // always join: nothing of the side stream may outlive this call
+      if (cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess && e == MGT_OK) e = MGT_ERR_CUDA;
+      if (e != MGT_OK) return e;
     }
-    // A[P0:, P0:] -= L21 U12 of block J0: the operand splits (the rows of L21
-    // are permuted by the next panels' interchanges) and the next block's
-    // columns here; the rest of the update on the side stream
-    e = lookahead_update(J0, W, P0, WN, rest, side->s);
-    if (e == MGT_OK) e = block_panels(P0, P0 + WN);
-    // always join: nothing of the side stream may outlive this call
-    if (cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess && e == MGT_OK) e = MGT_ERR_CUDA;
-    if (e != MGT_OK) return e;
     block_right(P0);
+    K0 = P0;
+    KW = WN;
+    const int Y0 = P0 + WN, WY = std::min(2 * NB, n - Y0);
+    if (pairs && WN == 2 * NB && WY == 2 * NB && n - P0 >= opt.wide_min) {
+      e = pair_update(P0, Y0, WY);
+      if (e == MGT_OK) e = block_panels(Y0, n);
+      if (e != MGT_OK) return e;
+      block_right(Y0);
+      KW = WN + WY;
+    }
   }
   return finish(2 * NB);
 }
@@ -2335,6 +2383,11 @@ extern "C" int mgt_set_tuning(int key, int value) {
     return MGT_OK;
   }
   if (key == MGT_TUNE_SYM_ASSEMBLY) return set_sym_assembly(value);
+  if (key == MGT_TUNE_WIDE_UPDATE) {
+    if (value < 0) return MGT_ERR_ARG;
+    g_wide_min.store(value);
+    return MGT_OK;
+  }
   return MGT_ERR_ARG;
 }
 
@@ -2349,5 +2402,6 @@ extern "C" int mgt_get_tuning(int key) {
   if (key == MGT_TUNE_FUSED_RIGHT) return g_fused_right.load();
   if (key == MGT_TUNE_PANEL_CLUSTER) return g_panel_cluster.load();
   if (key == MGT_TUNE_SYM_ASSEMBLY) return get_sym_assembly();
+  if (key == MGT_TUNE_WIDE_UPDATE) return g_wide_min.load();
   return MGT_ERR_ARG;
 }

@@ -114,7 +114,7 @@ def test_tuning_keys_round_trip_and_range_checks():
             L.MGT_TUNE_PANEL_MAX_CTAS: (40, [-1]), L.MGT_TUNE_PANEL_REGISTERS: (2, [3, -1]),
             L.MGT_TUNE_TC_PRECISION: (L.MGT_TC_TF32X3, [5]), L.MGT_TUNE_COOPERATIVE: (0, []),
             L.MGT_TUNE_LOOKAHEAD: (0, []), L.MGT_TUNE_FUSED_RIGHT: (0, []), L.MGT_TUNE_PANEL_CLUSTER: (0, []),
-            L.MGT_TUNE_SYM_ASSEMBLY: (0, [])}
+            L.MGT_TUNE_SYM_ASSEMBLY: (0, []), L.MGT_TUNE_WIDE_UPDATE: (4096, [-1])}
     saved = {k: lib.mgt_get_tuning(k) for k in keys}
     try:
         for k, (good, bad) in keys.items():

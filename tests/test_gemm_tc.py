@@ -22,7 +22,8 @@ def tc_mode(request):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 64), (1000, 700, 64), (257, 1029, 17),
-                                   (4096, 4096, 64), (129, 33, 1), (640, 520, 128)])
+                                   (4096, 4096, 64), (129, 33, 1), (640, 520, 128),
+                                   (700, 450, 256), (333, 530, 200), (1100, 260, 129)])
 def test_tc_update_matches_complex128(M, N, K, tc_mode):
     from magreete_gb300 import engine as E
     g = torch.Generator().manual_seed(M * 7 + N * 3 + K)
@@ -37,8 +38,10 @@ def test_tc_update_matches_complex128(M, N, K, tc_mode):
     Cbuf[:, :N] = C32.cuda()
     out = E.cgemm_sub(Cbuf[:, :N], A32.cuda(), B32.cuda(), tensor_cores=True)
     err = rel(out.cpu().to(torch.complex128), ref)
-    # FP32-level: the complex64 rounding of the result dominates
-    assert err < 2e-6, err
+    # FP32-level: the complex64 rounding of the result dominates for F16x2;
+    # TF32x3 keeps about 21 bits per product, an error that grows like sqrt(K)
+    tol = 2e-6 if tc_mode == "f16x2" else max(2e-6, 3e-7 * K ** 0.5)
+    assert err < tol, err
     assert torch.all(Cbuf[:, N:] == 0)   # padding columns keep their values
     simt = E.cgemm_sub(C32.clone().cuda(), A32.cuda(), B32.cuda(), tensor_cores=False)
     assert rel(simt.cpu().to(torch.complex128), ref) < 2e-6

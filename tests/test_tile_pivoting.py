@@ -62,6 +62,50 @@ def test_tile_lu_is_a_factorisation(kind, N, k):
         assert rel(Lm @ U, A[perm]) < 5e-8 * n * growth, growth
 
 
+@pytest.mark.parametrize("kind,N,k", [("2d", 1500, 20.0), ("3d", 1700, 10.0)])
+def test_tile_lu_paired_blocks(kind, N, k):
+    """Paired 128-wide blocks (the columns right of a pair take one K = 256
+    update; forced at these orders by lowering MGT_TUNE_WIDE_UPDATE): the same
+    factorisation property, and refined solves that agree with those of the
+    unpaired schedule."""
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import engine as E
+    from magreete_gb300 import serve
+    lib = L.load()
+    prob, pts, coef, shift, Mdf, M32 = _system64(kind, N, 9, k)
+    n = prob.n
+    A = M32.clone().to(torch.complex128)
+    opts = L.LuOptions(pivoting=L.MGT_PIVOT_TILE, outer_block=128, lookahead=1)
+    old = lib.mgt_get_tuning(L.MGT_TUNE_WIDE_UPDATE)
+    try:
+        lib.mgt_set_tuning(L.MGT_TUNE_WIDE_UPDATE, 256)
+        fw = E.lu_factor(M32.clone(), check_singular=False, options=opts)
+        lib.mgt_set_tuning(L.MGT_TUNE_WIDE_UPDATE, 0)
+        f1 = E.lu_factor(M32.clone(), check_singular=False, options=opts)
+    finally:
+        lib.mgt_set_tuning(L.MGT_TUNE_WIDE_UPDATE, old)
+    assert E.lu_info(fw) == (0, 0)
+    perm = fw.perm.long()
+    idx = torch.arange(n, device="cuda")
+    assert torch.equal(perm // 64, idx // 64)
+    assert torch.equal(torch.sort(perm).values, idx)
+    LU = fw.lu.to(torch.complex128)
+    Lm = torch.tril(LU, -1) + torch.eye(n, dtype=torch.complex128, device="cuda")
+    U = torch.triu(LU)
+    growth = max(1.0, (U.abs().max() / A.abs().max()).item())
+    assert rel(Lm @ U, A[perm]) < 5e-8 * n * growth, growth
+    # the two schedules differ only in the rounding of the updates (which can
+    # flip a near-tie between two pivot candidates)
+    if torch.equal(fw.perm, f1.perm):
+        assert rel(fw.lu, f1.lu) < 1e-4
+    E0s, _ = serve.incident_fields(prob, pts, prob.detectors.cuda())
+    B = E0s.reshape(n, -1).contiguous()
+    Xw, it_w, rr_w = E.solve_refined(Mdf, fw, B)
+    X1, it_1, rr_1 = E.solve_refined(Mdf, f1, B)
+    assert rr_w <= 1e-10 and rr_1 <= 1e-10
+    assert rel(Xw, X1) < 1e-9
+
+
 @pytest.mark.parametrize("kind,N,k", [("2d", 1000, 20.0), ("3d", 1400, 10.0)])
 def test_tile_pivoted_refined_solve_matches_partial(kind, N, k):
     """Refined solves from tile-pivoted and partially pivoted factors agree
