@@ -46,9 +46,9 @@ WORKLOAD = ("serving stream (continuous batching, 4 requests in flight): Poisson
             "detectors 360 ring (2D) / 1024 Fibonacci sphere (3D)")
 METRIC = "solves/s (mixed-N 2D/3D request stream, refined to 1e-10 relative residual)"
 # DRAM bytes / algorithmic bytes of the trailing update, from an ncu capture of one
-# full-size launch (3D N=4000, M = 11264, N = 11136 complex, K = 128: 2.009 GB of DRAM
-# traffic vs 2.03 GB algorithmic)
-TRAFFIC_RATIO = 0.99
+# full-size launch (3D N=4000, M = 11616, N = 8032 complex, K = 256: 1.575 GB of DRAM
+# traffic vs 1.533 GB algorithmic)
+TRAFFIC_RATIO = 1.03
 
 
 def parse():
@@ -585,7 +585,9 @@ def run_ours(args, rank, world, local):
         e_el = max_over_ranks(e_el, world, dev)
         e2e = {"value": n_req / e_el, "unit": "solves/s", "h2d_bytes_per_step": h2d // args.steps,
                "d2h_bytes_per_step": d2h // args.steps, "api": "magreete_gb300.serve.Server(host_results=True)"}
-        # the first timed window through the drop-in classes, one request at a time
+        # the first timed window through the drop-in classes, one request at a
+        # time, after one untimed pass over it (the classes' first-use costs)
+        e2e_class_api(wins[args.warmup], args.precision)
         t_api, h2d_api, d2h_api = e2e_class_api(wins[args.warmup], args.precision)
         e2e_api = {"value": len(wins[args.warmup]) / t_api, "unit": "solves/s", "requests": len(wins[args.warmup]),
                    "h2d_bytes": h2d_api, "d2h_bytes": d2h_api,
@@ -596,18 +598,30 @@ def run_ours(args, rank, world, local):
             torch.distributed.destroy_process_group()
         return
     hbm, bf16, src = measured_peaks()
-    # The trailing update reads and writes C once per K <= 128 (8 K flops per 16 B
-    # of complex64 C): its HBM ceiling (~64 flop/B x copy bandwidth) lies below its
-    # tensor ceiling (three F16 split products per flop), so the binding roofline
-    # is HBM, and achieved is algorithmic bytes / launch time.
+    # The trailing update's windows run with K = 128 (one block) or K = 256 (a
+    # pair of blocks).  Per algorithmic flop a window moves 16 B of complex64 C
+    # per 8 K flops and issues three F16 split products, so its roof is the
+    # larger of (algorithmic bytes / copy bandwidth) and (3 x flops / bf16
+    # peak): HBM at K = 128, tensor at K = 256.  For the windows together the
+    # larger of the two totals is taken (a lower bound of the roof time, so
+    # the fraction is conservative).
     gbs = (dom_bytes / (dom_ms * 1e-3) / 1e9) if dom_ms > 0 else None
     tflops = (dom_flops / (dom_ms * 1e-3) / 1e12) if dom_ms > 0 else None
+    t_hbm = dom_bytes / (hbm * 1e9) if hbm else 0.0
+    t_tc = 3 * dom_flops / (bf16 * 1e12) if bf16 else 0.0
+    tensor_bound = t_tc >= t_hbm
     roofline = {"kernel": "tc::cgemm_split3_kernel<F16x2> + operand splits (LU trailing update, tcgen05 kind::f16, "
-                          "K = 128)",
-                "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                "frac": (gbs / hbm) if gbs else None,
+                          "128 x 256 tiles, K = 256 for paired blocks, else 128)",
+                "bound": "tensor" if tensor_bound else "hbm",
+                "achieved": tflops if tensor_bound else gbs,
+                "peak": bf16 / 3 if tensor_bound else hbm,
+                "unit": "TFLOP/s" if tensor_bound else "GB/s",
+                "frac": ((t_tc if tensor_bound else t_hbm) / (dom_ms * 1e-3)) if dom_ms > 0 else None,
+                "hbm_achieved_gbs": gbs, "hbm_peak_gbs": hbm,
+                "hbm_frac": (gbs / hbm) if gbs else None,
                 "traffic": (dom_bytes / dom_n * TRAFFIC_RATIO) if dom_n else None,
-                "peak_source": f"hbm_gbs of {src} peaks (copy bandwidth)",
+                "peak_source": (f"bf16_tflops of {src} peaks / 3 (three kind::f16 split products per algorithmic "
+                                f"flop)" if tensor_bound else f"hbm_gbs of {src} peaks (copy bandwidth)"),
                 "algorithmic_bytes_per_launch": dom_bytes / dom_n if dom_n else None,
                 "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None,
                 "launches": dom_n, "avg_launch_ms": dom_ms / dom_n if dom_n else None,

@@ -1978,11 +1978,13 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       if (e == MGT_OK) e = tc_split_b(tc->plan, WN, W, U12, lda, s);
       if (e == MGT_OK) e = tc_gemm(tc->plan, tc->cmap, M, WN, W, 2 * P0, P0, ws.status, s);
       dom_end(s, 8.0 * M * (double)WN * W, sizeof(V) * (2.0 * M * (double)WN + (double)M * W + (double)W * WN));
-      if (e == MGT_OK) e = tc_split_b(tc->plan, rest, W, U12 + WN, lda, s);
       if (e != MGT_OK) return e;
       if (cudaEventRecord(side->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, side->fork, 0) != cudaSuccess)
         return MGT_ERR_CUDA;
+      // the rest's B split on the side stream too (this stream touches no
+      // split buffer before the join)
       dom_begin(s2);
+      e = tc_split_b(tc->plan, rest, W, U12 + WN, lda, s2);
       // the first columns beside the next block's panels, on the SMs they
       // leave free; the rest, by when the panels should be done, on every SM
       // (a persistent launch keeps the SMs it started on)
@@ -1991,7 +1993,8 @@ static int lu_factor_impl(cplx<T>* A, int n, int64_t lda, int32_t* perm, void* w
       const double t_pan = tile ? 3e-4 : 2.0 * NB * 4.5e-6 + 1e-4;
       const double head = t_pan * 3e14 * (sms - reserve) / sms / (8.0 * M * (double)W);
       const int c1 = (int)std::min<double>(rest, (std::floor(head / (2 * NB)) + 1) * (2 * NB));
-      e = tc_gemm(tc->plan, tc->cmap, M, c1, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - reserve));
+      if (e == MGT_OK)
+        e = tc_gemm(tc->plan, tc->cmap, M, c1, W, 2 * (P0 + WN), P0, ws.status, s2, std::max(1, sms - reserve));
       if (e == MGT_OK && c1 < rest)
         e = tc_gemm(tc->plan, tc->cmap, M, rest - c1, W, 2 * (P0 + WN + c1), P0, ws.status, s2, 0, c1);
       dom_end(s2, 8.0 * M * (double)rest * W, sizeof(V) * (2.0 * M * (double)rest + (double)W * rest));
