@@ -203,11 +203,19 @@ __device__ __forceinline__ void tri_stage(V* buf, int st, int ndep, const V* __r
 // stages are the factor blocks it depends on, then its inverted diagonal
 // block; each is copied asynchronously, and with two buffers the next stage
 // loads while the current block product runs.
+// Split sums: each (block row, group) is `parts` items, claimed helpers
+// first.  Helper p >= 1 sums the products of dependencies
+// [last - (p+1) dper, last - p dper) into its slot of `part` and releases its
+// flag in `hflags`; the main item (p = 0) sums the dper dependencies before
+// the last, adds the helpers' slots, then solves as above.  A row's long sum
+// of block products is thus spread over `parts` CTAs.  Every item waits only
+// on items claimed before it, so progress is guaranteed as before.
 template <typename T, bool UPPER, int TG>
 __global__ void __launch_bounds__(256)
 tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __restrict__ Inv,
                  const cplx<T>* __restrict__ W, cplx<T>* __restrict__ X, int64_t ldx, int n, int ncols,
-                 unsigned* counter, unsigned* flags, const unsigned* epoch_ptr, int* status) {
+                 unsigned* counter, unsigned* flags, const unsigned* epoch_ptr, int* status, int parts, int dper,
+                 cplx<T>* __restrict__ part, unsigned* hflags) {
   // flag value of this solve: bumped on the device before the launch, so a
   // replay from a CUDA graph never sees the previous run's flags as ready
   const unsigned epoch = *(volatile const unsigned*)epoch_ptr;
@@ -222,29 +230,27 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
   __shared__ int s_fail;
   const int tid = threadIdx.x, tr = tid / TPR, tc = tid % TPR;
   const int nb = (n + kTB - 1) / kTB, ng = (ncols + TG - 1) / TG;
-  const unsigned items = (unsigned)nb * ng;
+  const unsigned items = (unsigned)nb * ng * parts;
   while (true) {
     if (tid == 0) { s_item = atomicAdd(counter, 1u); s_fail = 0; }
     __syncthreads();
     const unsigned k = s_item;
     if (k >= items) break;
-    const int kr = (int)(k / ng), g = (int)(k % ng);
+    const unsigned rg = k / parts;
+    const int p = parts - 1 - (int)(k % parts);   // helpers (p >= 1, farthest first), then the main item
+    const int kr = (int)(rg / ng), g = (int)(rg % ng);
     const int i = UPPER ? nb - 1 - kr : kr;
     const int r0 = i * kTB, rb = min(kTB, n - r0), cg = g * TG;
     unsigned* gflags = flags + (size_t)g * nb;
-    V acc[TR][TC];
-#pragma unroll
-    for (int a = 0; a < TR; ++a)
-#pragma unroll
-      for (int b = 0; b < TC; ++b) {
-        const int r = TR * tr + a, c = cg + tc + TPR * b;
-        acc[a][b] = (r < rb && c < ncols) ? X[(int64_t)(r0 + r) * ldx + c] : czero<V>();
-      }
     // dependencies in completion order: ascending for L, descending for U.
     // All but the last are applied as they complete; then Z = Inv_i acc is
     // formed before the last one is done, and after it X_i = Z - W_i X_last:
     // one product on the chain from block to block instead of two.
     const int ndep = UPPER ? nb - 1 - i : i;
+    // dependencies [dlo(q), dhi(q)) of part q (the last one, ndep - 1, is the main item's)
+    auto dlo = [&](int q) { return max(0, ndep - 1 - (q + 1) * dper); };
+    auto dhi = [&](int q) { return max(0, ndep - 1 - q * dper); };
+    const size_t slot = ((size_t)i * ng + g) * (parts - 1);   // + q - 1 for helper q
     auto stage = [&](V* buf, int st) { tri_stage<UPPER>(buf, st, ndep, F, ldf, Inv, W, i, nb, n, r0, rb, tid); };
     auto bufof = [&](int st) { return Asb + (NBUF == 2 ? (st & 1) * kAs : 0); };
     // wait for dependency d's completion flag and stage its rows of X in Ys
@@ -267,8 +273,51 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       __syncthreads();
       return true;
     };
-    stage(bufof(0), 0);
-    for (int d = 0; d < ndep - 1; ++d) {
+    V acc[TR][TC];
+    if (p > 0) {
+      // helper: -(sum of its dependencies' products) into its slot
+      const int lo = dlo(p), hi = dhi(p);
+      if (lo >= hi) {
+        __syncthreads();   // every thread has read s_item before it is claimed again
+        continue;
+      }
+#pragma unroll
+      for (int a = 0; a < TR; ++a)
+#pragma unroll
+        for (int b = 0; b < TC; ++b) acc[a][b] = czero<V>();
+      stage(bufof(lo), lo);
+      for (int d = lo; d < hi; ++d) {
+        const bool next = d + 1 < hi;
+        if (NBUF == 2 && next) stage(bufof(d + 1), d + 1);
+        if (NBUF == 2 && next) cp_async_wait<1>(); else cp_async_wait<0>();
+        if (!take_dep(d)) {
+          cp_async_wait<0>();
+          return;
+        }
+        block_gemm_sub<TG>(acc, bufof(d), Ys, tr, tc);
+        __syncthreads();
+        if (NBUF == 1 && next) stage(bufof(d + 1), d + 1);
+      }
+      V* out = part + (slot + p - 1) * (size_t)(kTB * TG);
+#pragma unroll
+      for (int a = 0; a < TR; ++a)
+#pragma unroll
+        for (int b = 0; b < TC; ++b) out[(TR * tr + a) * TG + tc + TPR * b] = acc[a][b];
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) st_release_u32(hflags + slot + p - 1, epoch);
+      continue;
+    }
+#pragma unroll
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TC; ++b) {
+        const int r = TR * tr + a, c = cg + tc + TPR * b;
+        acc[a][b] = (r < rb && c < ncols) ? X[(int64_t)(r0 + r) * ldx + c] : czero<V>();
+      }
+    const int d0 = dlo(0);
+    stage(bufof(d0), d0);
+    for (int d = d0; d < ndep - 1; ++d) {
       if (NBUF == 2) stage(bufof(d + 1), d + 1);
       if (NBUF == 2) cp_async_wait<1>(); else cp_async_wait<0>();
       if (!take_dep(d)) {
@@ -278,6 +327,30 @@ tri_solve_kernel(const cplx<T>* __restrict__ F, int64_t ldf, const cplx<T>* __re
       block_gemm_sub<TG>(acc, bufof(d), Ys, tr, tc);
       __syncthreads();
       if (NBUF == 1) stage(bufof(d + 1), d + 1);
+    }
+    // the helpers' sums (helpers beyond the first empty one are empty too)
+    for (int q = 1; q < parts && dlo(q) < dhi(q); ++q) {
+      if (tid == 0) {
+        unsigned it = 0;
+        while (ld_acquire_u32(hflags + slot + q - 1) != epoch) {
+          if (++it > kSpinLimit) { s_fail = 1; atomicExch(status, MGT_ERR_TIMEOUT); break; }
+          if (it > 64) __nanosleep(32);
+        }
+      }
+      __syncthreads();
+      if (s_fail) {
+        cp_async_wait<0>();
+        return;
+      }
+      const V* in = part + (slot + q - 1) * (size_t)(kTB * TG);
+#pragma unroll
+      for (int a = 0; a < TR; ++a)
+#pragma unroll
+        for (int b = 0; b < TC; ++b) {
+          const V v = ldcg(in + (TR * tr + a) * TG + tc + TPR * b);
+          acc[a][b].x += v.x;
+          acc[a][b].y += v.y;
+        }
     }
     // Z = Inv_i * acc (Inv_i is stage max(ndep - 1, 0)); W_i loads meanwhile
     const int sinv = ndep > 0 ? ndep - 1 : 0;
@@ -338,13 +411,29 @@ __global__ void tri_start_kernel(unsigned* counter, unsigned* mark, unsigned* fl
   for (int f = i; f < nflags; f += gridDim.x * blockDim.x) flags[f] = 0;
 }
 
-// counter + status (256 B), flags (groups x blocks), inverted diagonal blocks
-// (L and U) and the chain factors W (L and U)
-size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem) {
-  const int64_t nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG;
-  size_t flags = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
-  return 256 + flags + 2 * (size_t)nb * kTB * kTB * elem * 2;
-}
+// Items per (block row, column group): the main item and its helpers, for a
+// solve of nb block rows (the last rows' sums then take about nb / parts
+// block products in a row instead of nb)
+static int tri_parts(int64_t nb) { return nb >= 64 ? 4 : 1; }
+
+// Workspace of one triangular solve: counter, completion mark and status
+// (256 B); completion flags (groups x blocks) followed by the helpers' flags
+// (groups x blocks x (parts - 1)); inverted diagonal blocks (L and U); chain
+// factors W (L and U); the helpers' partial sums (64 x group width each).
+// Sized for the narrow groups (the most flags); a solve in wide groups fits.
+struct TriWs {
+  size_t flags = 256, inv, wch, part, total;
+  TriWs(int64_t n, int64_t nrhs, size_t elem) {
+    const int64_t nb = (n + kTB - 1) / kTB, ng = (nrhs + kTG - 1) / kTG, P = tri_parts(nb);
+    inv = flags + (((size_t)(nb * ng * P) * sizeof(unsigned) + 255) & ~size_t(255));
+    wch = inv + 2 * (size_t)nb * kTB * kTB * elem;
+    part = wch + 2 * (size_t)nb * kTB * kTB * elem;
+    const int64_t cols = (nrhs + kTGWide - 1) / kTGWide * kTGWide;   // >= groups x group width
+    total = part + (size_t)(nb * (P - 1)) * kTB * cols * elem;
+  }
+};
+
+size_t tri_solve_workspace_bytes(int64_t n, int64_t nrhs, size_t elem) { return TriWs(n, nrhs, elem).total; }
 
 static int resident_ctas(const void* kern, size_t smem) {
   int dev = 0, sms = 1, per = 1;
@@ -388,31 +477,38 @@ int tri_solve(const cplx<T>* F, int64_t ldf, cplx<T>* X, int64_t ldx, int n, int
   const bool wide = sizeof(T) == 4 && n >= kWideMinN;
   const int tg = wide ? kTGWide : kTG;
   const int nb = (n + kTB - 1) / kTB, ng = (nrhs + tg - 1) / tg;
+  const int parts = tri_parts(nb);
+  const int dper = parts > 1 ? (nb - 1 + parts - 1) / parts : std::max(1, nb);   // parts x dper >= nb - 1
+  const TriWs L(n, nrhs, sizeof(V));
   unsigned* counter = (unsigned*)work;
-  unsigned* flags = (unsigned*)((char*)work + 256);
-  size_t flag_bytes = ((size_t)(nb * ng) * sizeof(unsigned) + 255) & ~size_t(255);
+  unsigned* flags = (unsigned*)((char*)work + L.flags);
+  unsigned* hflags = flags + (size_t)nb * ng;
   // inverted diagonal blocks (L, then U), then the chain factors W (L, then U)
-  V* inv = (V*)((char*)work + 256 + flag_bytes) + (UPPER ? (size_t)nb * kTB * kTB : 0);
-  V* wch = (V*)((char*)work + 256 + flag_bytes) + 2 * (size_t)nb * kTB * kTB + (UPPER ? (size_t)nb * kTB * kTB : 0);
+  V* inv = (V*)((char*)work + L.inv) + (UPPER ? (size_t)nb * kTB * kTB : 0);
+  V* wch = (V*)((char*)work + L.wch) + (UPPER ? (size_t)nb * kTB * kTB : 0);
+  V* part = (V*)((char*)work + L.part);
   count_launch(2);
   diag_inverse_kernel<T, UPPER><<<nb, 256, smem_inv, s>>>(F, ldf, n, inv);
   chain_factor_kernel<T, UPPER><<<nb, 256, smem_cf, s>>>(F, ldf, n, inv, wch);
   unsigned* epoch = counter + 1;   // completion mark, set by tri_start_kernel
+  const int nflags = nb * ng * parts;
+  const int64_t items = (int64_t)nb * ng * parts;
   count_launch();
-  tri_start_kernel<<<std::max(1, std::min(nb * ng, 1 << 16) / 256 + 1), 256, 0, s>>>(counter, epoch, flags, nb * ng);
+  tri_start_kernel<<<std::max(1, std::min(nflags, 1 << 16) / 256 + 1), 256, 0, s>>>(counter, epoch, flags, nflags);
   count_launch();
   if constexpr (sizeof(T) == 4) {
     if (wide) {
-      const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_w_dev[dev]));
+      const int grid = (int)std::min<int64_t>(items, std::max(1, max_ctas_w_dev[dev]));
       tri_solve_kernel<T, UPPER, kTGWide><<<grid, 256, smem_w, s>>>(F, ldf, inv, wch, X, ldx, n, nrhs, counter,
-                                                                     flags, epoch, status);
+                                                                     flags, epoch, status, parts, dper, part,
+                                                                     hflags);
       return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
     }
   }
   {
-    const int grid = (int)std::min<int64_t>((int64_t)nb * ng, std::max(1, max_ctas_dev[dev]));
+    const int grid = (int)std::min<int64_t>(items, std::max(1, max_ctas_dev[dev]));
     tri_solve_kernel<T, UPPER, kTG><<<grid, 256, smem, s>>>(F, ldf, inv, wch, X, ldx, n, nrhs, counter, flags,
-                                                             epoch, status);
+                                                             epoch, status, parts, dper, part, hflags);
   }
   return cudaGetLastError() == cudaSuccess ? MGT_OK : MGT_ERR_CUDA;
 }

@@ -266,17 +266,20 @@ def test_fused_block_right_matches_passes(n):
 @pytest.mark.gpu
 @pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
 @pytest.mark.parametrize("fill", ["iota", "small_ints", "ones"])
-def test_lu_solve_any_workspace_contents(dtype, fill):
-    """The triangular solves' completion flags live in the caller's workspace:
-    whatever it held before (a freed permutation holds every small integer)
-    must not mark a block as solved."""
+@pytest.mark.parametrize("n", [1500, 5000])
+def test_lu_solve_any_workspace_contents(dtype, fill, n):
+    """The triangular solves' completion flags (and, at n = 5000, where each
+    block row's sum is split over four work items, the helpers' flags and
+    partial sums) live in the caller's workspace: whatever it held before (a
+    freed permutation holds every small integer) must not mark a block or a
+    partial sum as done."""
     import ctypes
     from magreete_gb300 import _lib as L
     from magreete_gb300 import engine as E
     lib = L.load()
-    n, R = 1500, 40
+    R = 40
     gen = torch.Generator().manual_seed(3)
-    A = torch.randn(n, n, dtype=torch.complex128, generator=gen) + 40 * torch.eye(n)
+    A = torch.randn(n, n, dtype=torch.complex128, generator=gen) + (4 * n ** 0.5) * torch.eye(n)
     B = torch.randn(n, R, dtype=torch.complex128, generator=gen)
     f = E.lu_factor(A.to(dtype).cuda())
     nb = ctypes.c_size_t()
