@@ -76,7 +76,9 @@ def solve_problem(prob, precision="mixed", pts=None, det=None, tol=E.DEFAULT_TOL
 def matrix_bytes(prob, precision="mixed"):
     """Device bytes a request holds at its peak: the matrix copies (24 B / entry
     mixed: complex64 LU + double-float residual copy; 16 B fp64), the
-    tensor-core split buffers (3 KB per row), the right-hand-side blocks and
+    tensor-core split buffers of the LU's update (12 KB per row: K up to 256,
+    sized for fp32 splits), the triangular solves' partial sums (24 B per row
+    and right-hand side, rounded up to 64 of them), the right-hand-side blocks and
     the propagation workspace (double-float propagator rows, at most 1 GiB at
     a time, and the double-float copy of the fields), the split-K partial sums
     of the residual (at most 16 splits) and the digits of the tensor-core
@@ -92,7 +94,8 @@ def matrix_bytes(prob, precision="mixed"):
     digits = 57344 * -(-n // 32) * -(-R // 32)
     if precision != "fp64":
         digits += 14 * (-(-n // 128) * 128) * (-(-n // 32) * 32)
-    return per * n * n + 3072 * n + 8 * 16 * n * R + prop + partial + digits + (64 << 20)
+    split = 12288 * n + 24 * n * (-(-R // 64) * 64)
+    return per * n * n + split + 8 * 16 * n * R + prop + partial + digits + (64 << 20)
 
 
 def serve_sequential(problems, precision="mixed", device_inputs=None, start=None):
