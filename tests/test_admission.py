@@ -109,3 +109,40 @@ def test_many_workers_never_exceed_budget():
         w.join(10)
     assert sorted(done) == list(range(len(needs)))
     assert peak[0] <= 100 and adm.in_use == 0
+
+
+@pytest.mark.parametrize("kind,N,R,T", [("2d_vector", 1026, 1, 360), ("2d_vector", 8000, 16, 360),
+                                        ("3d_vector", 4000, 64, 1024), ("3d_vector", 14420, 64, 1024),
+                                        ("3d_vector", 20000, 128, 1024)])
+def test_request_estimate_covers_the_library_workspaces(kind, N, R, T):
+    """serve.matrix_bytes, the HBM a request is admitted with, covers what the
+    library's own workspace queries ask for at the request's peak: the
+    matrix copies (24 B per entry) with the refinement workspace (the
+    residual's digits, the right-hand-side blocks, the triangular solves'
+    workspace) and the LU's (its tensor-core split buffers), and the
+    propagation workspace.  Host-only queries: no GPU needed."""
+    import ctypes
+    from types import SimpleNamespace
+    import torch
+    from magreete_gb300 import _lib as L
+    from magreete_gb300 import serve
+    import os
+    if not os.path.exists(L.LIB_PATH):
+        pytest.skip("library not built")
+    lib = L.load()
+    d = 2 if kind.startswith("2d") else 3
+    n = d * N
+
+    def q(fn, *args):
+        nb = ctypes.c_size_t()
+        L.check(fn(*args, ctypes.byref(nb)))
+        return nb.value
+
+    prob = SimpleNamespace(kind=kind, n=n, nrhs=R, d=d, detectors=torch.zeros(T, d))
+    est = serve.matrix_bytes(prob, "mixed")
+    refine = q(lib.mgt_refine_workspace_bytes, n, R)
+    lu = q(lib.mgt_lu_workspace_bytes, L.MGT_C64, n)
+    prop = q(lib.mgt_propagate_workspace_bytes, L.KIND_CODE[kind] if hasattr(L, "KIND_CODE") else
+             {"2d_vector": L.MGT_2D_VECTOR, "3d_vector": L.MGT_3D_VECTOR}[kind], T, N, R)
+    assert est >= 24 * n * n + refine + lu, (est, refine, lu)
+    assert est >= 8 * n * n + prop + 16 * n * R
