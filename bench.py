@@ -391,6 +391,44 @@ def vs_plain_fp64(srv, wins, dev_inputs):
             "max_field_err_vs_fp64": {"Ek": max(ek), "E_det": max(ed)}}
 
 
+def update_roofline(dom_n, dom_ms, dom_flops, dom_bytes, hbm, bf16, src):
+    """Roofline entry of the trailing update from its timed windows (count,
+    total ms, algorithmic flops and bytes) and the measured peaks (copy GB/s,
+    bf16 TFLOP/s).  The windows run with K = 128 (one block) or K = 256 (a
+    pair of blocks).  Per algorithmic flop a window moves 16 B of complex64 C
+    per 8 K flops and issues three F16 split products, so its roof is the
+    larger of (algorithmic bytes / copy bandwidth) and (3 x flops / bf16
+    peak): HBM at K = 128, tensor at K = 256.  For the windows together the
+    larger of the two totals is taken (a lower bound of the roof time, so the
+    fraction is conservative)."""
+    gbs = (dom_bytes / (dom_ms * 1e-3) / 1e9) if dom_ms > 0 else None
+    tflops = (dom_flops / (dom_ms * 1e-3) / 1e12) if dom_ms > 0 else None
+    t_hbm = dom_bytes / (hbm * 1e9) if hbm else 0.0
+    t_tc = 3 * dom_flops / (bf16 * 1e12) if bf16 else 0.0
+    tensor_bound = t_tc >= t_hbm
+    return {"kernel": "tc::cgemm_split3_kernel<F16x2> + operand splits (LU trailing update, tcgen05 kind::f16, "
+                      "128 x 256 tiles, K = 256 for paired blocks, else 128)",
+            "bound": "tensor" if tensor_bound else "hbm",
+            "achieved": tflops if tensor_bound else gbs,
+            "peak": bf16 / 3 if tensor_bound else hbm,
+            "unit": "TFLOP/s" if tensor_bound else "GB/s",
+            "frac": ((t_tc if tensor_bound else t_hbm) / (dom_ms * 1e-3)) if dom_ms > 0 else None,
+            "hbm_achieved_gbs": gbs, "hbm_peak_gbs": hbm,
+            "hbm_frac": (gbs / hbm) if gbs else None,
+            "traffic": (dom_bytes / dom_n * TRAFFIC_RATIO) if dom_n else None,
+            "peak_source": (f"bf16_tflops of {src} peaks / 3 (three kind::f16 split products per algorithmic "
+                            f"flop)" if tensor_bound else f"hbm_gbs of {src} peaks (copy bandwidth)"),
+            "algorithmic_bytes_per_launch": dom_bytes / dom_n if dom_n else None,
+            "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None,
+            "launches": dom_n, "avg_launch_ms": dom_ms / dom_n if dom_n else None,
+            "achieved_tflops": tflops,
+            "tensor_peak_tflops": bf16,
+            "tensor_frac": (3 * tflops / bf16) if tflops else None,
+            "tensor_note": "three kind::f16 split products per algorithmic flop; tensor_frac = 3 x achieved / "
+                           f"bf16_tflops of {src} peaks",
+            "measured": "CUDA events around each launch on its stream, sequential pass over the first timed window"}
+
+
 def secondary_rooflines():
     """The two other kernels with large shares of the stream, timed alone with
     CUDA events after the timed region:
@@ -601,40 +639,8 @@ def run_ours(args, rank, world, local):
             torch.distributed.destroy_process_group()
         return
     hbm, bf16, src = measured_peaks()
-    # The trailing update's windows run with K = 128 (one block) or K = 256 (a
-    # pair of blocks).  Per algorithmic flop a window moves 16 B of complex64 C
-    # per 8 K flops and issues three F16 split products, so its roof is the
-    # larger of (algorithmic bytes / copy bandwidth) and (3 x flops / bf16
-    # peak): HBM at K = 128, tensor at K = 256.  For the windows together the
-    # larger of the two totals is taken (a lower bound of the roof time, so
-    # the fraction is conservative).
-    gbs = (dom_bytes / (dom_ms * 1e-3) / 1e9) if dom_ms > 0 else None
-    tflops = (dom_flops / (dom_ms * 1e-3) / 1e12) if dom_ms > 0 else None
-    t_hbm = dom_bytes / (hbm * 1e9) if hbm else 0.0
-    t_tc = 3 * dom_flops / (bf16 * 1e12) if bf16 else 0.0
-    tensor_bound = t_tc >= t_hbm
-    roofline = {"kernel": "tc::cgemm_split3_kernel<F16x2> + operand splits (LU trailing update, tcgen05 kind::f16, "
-                          "128 x 256 tiles, K = 256 for paired blocks, else 128)",
-                "bound": "tensor" if tensor_bound else "hbm",
-                "achieved": tflops if tensor_bound else gbs,
-                "peak": bf16 / 3 if tensor_bound else hbm,
-                "unit": "TFLOP/s" if tensor_bound else "GB/s",
-                "frac": ((t_tc if tensor_bound else t_hbm) / (dom_ms * 1e-3)) if dom_ms > 0 else None,
-                "hbm_achieved_gbs": gbs, "hbm_peak_gbs": hbm,
-                "hbm_frac": (gbs / hbm) if gbs else None,
-                "traffic": (dom_bytes / dom_n * TRAFFIC_RATIO) if dom_n else None,
-                "peak_source": (f"bf16_tflops of {src} peaks / 3 (three kind::f16 split products per algorithmic "
-                                f"flop)" if tensor_bound else f"hbm_gbs of {src} peaks (copy bandwidth)"),
-                "algorithmic_bytes_per_launch": dom_bytes / dom_n if dom_n else None,
-                "algorithmic_flops_per_launch": dom_flops / dom_n if dom_n else None,
-                "launches": dom_n, "avg_launch_ms": dom_ms / dom_n if dom_n else None,
-                "achieved_tflops": tflops,
-                "tensor_peak_tflops": bf16,
-                "tensor_frac": (3 * tflops / bf16) if tflops else None,
-                "tensor_note": "three kind::f16 split products per algorithmic flop; tensor_frac = 3 x achieved / "
-                               f"bf16_tflops of {src} peaks",
-                "measured": "CUDA events around each launch on its stream, sequential pass over the first timed window",
-                "in_mix_tflops": (mix_flops / (mix_ms * 1e-3) / 1e12) if mix_ms > 0 else None}
+    roofline = update_roofline(dom_n, dom_ms, dom_flops, dom_bytes, hbm, bf16, src)
+    roofline["in_mix_tflops"] = (mix_flops / (mix_ms * 1e-3) / 1e12) if mix_ms > 0 else None
     secondary = secondary_rooflines()
     sweep = None if args.no_extras else sweep_measure(256, 32)
     cpu = cpu_extra = None

@@ -120,3 +120,35 @@ def test_bench_names_are_all_defined():
             bound.add(node.name)
     used = {n.id for n in ast.walk(tree) if isinstance(n, ast.Name) and isinstance(n.ctx, ast.Load)}
     assert not (used - bound), sorted(used - bound)
+
+
+def test_update_roofline_bound_follows_k():
+    """The trailing update's roofline entry: a K = 128 window (16 B of C per
+    64 flops) is HBM-bound, a K = 256 window tensor-bound (three F16 split
+    products per flop against bf16 / 3); frac = roof time / measured time."""
+    import bench
+    hbm, bf16 = 6681.8, 1913.9
+    M = N = 10000
+
+    def window(K, ms):
+        return 1, ms, 8.0 * M * N * K, 8.0 * (2 * M * N + K * (M + N))
+
+    n, ms, fl, by = window(128, 0.5)
+    r = bench.update_roofline(n, ms, fl, by, hbm, bf16, "measured")
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["peak"] == hbm
+    assert r["frac"] == pytest.approx(by / (hbm * 1e9) / (ms * 1e-3))
+    assert r["achieved"] == pytest.approx(by / (ms * 1e-3) / 1e9)
+    n, ms, fl, by = window(256, 0.5)
+    r = bench.update_roofline(n, ms, fl, by, hbm, bf16, "measured")
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s" and r["peak"] == pytest.approx(bf16 / 3)
+    assert r["frac"] == pytest.approx(3 * fl / (bf16 * 1e12) / (ms * 1e-3))
+    assert r["tensor_frac"] == pytest.approx(r["frac"])
+    # windows of both kinds together: the larger of the two roof-time totals decides
+    # (here one K = 128 and one K = 256 window: HBM 0.488 ms against tensor 0.482 ms)
+    a, b = window(128, 0.5), window(256, 0.5)
+    fl, by = a[2] + b[2], a[3] + b[3]
+    t_hbm, t_tc = by / (hbm * 1e9), 3 * fl / (bf16 * 1e12)
+    r = bench.update_roofline(2, 1.0, fl, by, hbm, bf16, "measured")
+    assert r["bound"] == ("tensor" if t_tc >= t_hbm else "hbm")
+    assert r["frac"] == pytest.approx(max(t_hbm, t_tc) / 1e-3)
+    assert bench.update_roofline(0, 0.0, 0.0, 0.0, hbm, bf16, "measured")["frac"] is None
