@@ -24,6 +24,7 @@ import torch
 
 from . import engine as E
 from . import selfterm
+from . import spectral as SP
 
 
 def _as_tensor(x):
@@ -276,12 +277,65 @@ class CoupledDipoleSolver:
             outs.append(self._ldos_from_dots(dots, P, k0, alpha, discard_absorption))
         return torch.cat(outs).to(_home_device(batches[0] if len(batches) else None, self.r))
 
-    # ------------------------------------------------------------ out of scope
-    def compute_hamiltonian_DOS(self, *args, **kwargs):
-        raise NotImplementedError("spectral tools (dense non-Hermitian eigensolvers) are not part of this engine")
+    # ------------------------------------------------------------ spectral tools
+    # Dense non-Hermitian eigenproblems: the Green's matrix from the GPU
+    # assembly, LAPACK's eigensolver on the host as in the reference
+    # (spectral.py).  Results are returned on the device of the points.  The
+    # reference's plots of compute_eigenmodes_IPR (utils.plot_IPR_damping_values)
+    # are not drawn: no plotting library is part of this engine.
+    def _spectral_system(self, k0, alpha, radius, self_interaction, si_type):
+        G = self._G0_dense(None, k0, "DOS eigvals")
+        return SP.system_matrix(G, k0, alpha, self._shift(k0, alpha, radius, self_interaction, si_type))
 
-    def compute_eigenvalues_and_scatterer_LDOS(self, *args, **kwargs):
-        raise NotImplementedError("spectral tools (dense non-Hermitian eigensolvers) are not part of this engine")
+    def compute_hamiltonian_DOS(self, k0, deltas, file_name, write_eigenvalues=True):
+        """DOS of the near-resonant Hamiltonian built from the scatterer Green's
+        matrix, at the detunings `deltas` (Transmission2D.py:455-477, :955-977;
+        Transmission3D.py:442-464, :951-973).  Writes the eigenvalues to
+        <file_name>_hamiltonian_lambdas_<k0L/2pi>_vector.csv (the name every
+        reference class uses)."""
+        k0_ = self._k_label(k0)
+        self._say(f"Computing Hamiltonian DOS od {self.N} points at k0L/2pi = {k0_}")
+        dos, lambdas = SP.hamiltonian_dos(self.kind, self._G0_dense(None, k0, "Hamiltonian DOS"), k0, deltas)
+        if write_eigenvalues:
+            np.savetxt(file_name + "_hamiltonian_lambdas_" + k0_ + "_vector.csv",
+                       np.stack([lambdas.real.numpy(), lambdas.imag.numpy()]).T)
+        return dos.to(_home_device(self.r))
 
-    def compute_eigenmodes_IPR(self, *args, **kwargs):
-        raise NotImplementedError("spectral tools (dense non-Hermitian eigensolvers) are not part of this engine")
+    def compute_eigenvalues_and_scatterer_LDOS(self, k0, alpha, radius, file_name, self_interaction=True,
+                                               self_interaction_type="Rayleigh", write_eigenvalues=True):
+        """The LDOS at the scatterers from the eigenvalues d of the system
+        matrix, Im(c sum((1 - d)^2 / d) / N) (Transmission2D.py:479-515,
+        :979-1015; Transmission3D.py:466-501, :975-1009).  Writes the
+        eigenvalues to <file_name>_deltas_<k0L/2pi>[_vector|_scalar].csv as the
+        reference names them."""
+        k0_ = self._k_label(k0)
+        self._say(f"Computing spectrum and scatterer LDOS using {self.N} points at k0L/2pi = {k0_}")
+        M = self._spectral_system(k0, alpha, radius, self_interaction, self_interaction_type)
+        factor, deltas = SP.scatterer_ldos_factor(self.kind, M, self.N, k0, alpha)
+        if write_eigenvalues:
+            suffix = {"2d_vector": "_vector.csv", "2d_scalar": "_scalar.csv"}.get(self.kind, ".csv")
+            np.savetxt(file_name + "_deltas_" + k0_ + suffix, np.stack([deltas.real.numpy(), deltas.imag.numpy()]).T)
+        return factor.to(_home_device(self.r))
+
+    def compute_eigenmodes_IPR(self, k0, alpha, radius, file_name, self_interaction=True,
+                               self_interaction_type="Rayleigh", number_eigenmodes=1, write_eigenvalues=True,
+                               sorting_type="IPR"):
+        """Eigenmodes of the system matrix with their inverse participation
+        ratios, sorted by IPR or by damping (Transmission2D.py:517-569,
+        :1017-1060; Transmission3D.py:503-564, :1011-1070).  Returns (values,
+        the first number_eigenmodes eigenvectors, IPRs); the unsorted values
+        and IPRs go to <file_name>_deltas_<k0L/2pi>.csv (2D) or
+        <file_name>_lambdas_<k0L/2pi>.csv (3D)."""
+        k0_ = self._k_label(k0)
+        self._say(f"Computing spectrum and scatterer LDOS using {self.N} points at k0L/2pi = {k0_}")
+        M = self._spectral_system(k0, alpha, radius, self_interaction, self_interaction_type)
+        values, vectors, iprs = SP.eigenmodes(self.kind, M, k0, alpha, radius)
+        if write_eigenvalues:
+            name = "_deltas_" if self.kind.startswith("2d") else "_lambdas_"
+            np.savetxt(file_name + name + k0_ + ".csv",
+                       np.stack([values.real.numpy(), values.imag.numpy(), iprs.numpy()]).T)
+        values, vectors, iprs = SP.sort_modes(values, vectors, iprs, sorting_type)
+        if self.kind.startswith("3d"):
+            self._say(str(SP.mean_resonance_ratio(self.kind, values, k0, alpha, radius)))
+        home = _home_device(self.r)
+        return values.to(home), vectors[:, 0:number_eigenmodes].to(home), iprs.to(home)

@@ -4,6 +4,7 @@ Run from the repository root on a machine that has the reference checkout:
 
     python tests/golden/make_golden.py /root/reference            # golden_<kind>.npz
     python tests/golden/make_golden.py /root/reference --greens   # golden_greens_<kind>.npz
+    python tests/golden/make_golden.py /root/reference --spectral # golden_spectral_<kind>.npz
 
 The reference imports ``hickle``, ``matplotlib`` and ``cmasher`` at module
 level; none of them is used on the solve path, so empty stand-in modules are
@@ -187,10 +188,71 @@ def main_greens(ref_path):
         print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def main_spectral(ref_path):
+    """golden_spectral_<kind>.npz: the spectral tools of each class
+    (compute_hamiltonian_DOS, compute_eigenvalues_and_scatterer_LDOS,
+    compute_eigenmodes_IPR with both sortings) on a small seeded pattern: their
+    return values and the CSV files they write.  The plots of
+    compute_eigenmodes_IPR (utils.plot_IPR_damping_values, matplotlib) are
+    replaced by a no-op."""
+    import tempfile
+    _stub_modules()
+    sys.path.insert(0, ref_path)
+    import torch
+    import utils
+    from Transmission2D import Transmission2D_vector, Transmission2D_scalar
+    from Transmission3D import Transmission3D_vector, Transmission3D_scalar
+    utils.plot_IPR_damping_values = lambda *a, **k: None
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    cases = {
+        "2d_vector": (Transmission2D_vector, 2, 40, 2 * np.pi * 4.0, 1.6 + 0.0j, 0.05),
+        "2d_scalar": (Transmission2D_scalar, 2, 40, 2 * np.pi * 4.0, 1.6 + 0.01j, 0.05),
+        "3d_vector": (Transmission3D_vector, 3, 24, 2 * np.pi * 2.0, 1.6 + 0.0j, 0.1),
+        "3d_scalar": (Transmission3D_scalar, 3, 24, 2 * np.pi * 2.0, 1.6 + 0.02j, 0.1),
+    }
+    for seed, (kind, (cls, dim, N, k0, n_ref, phi)) in enumerate(cases.items()):
+        rng = np.random.default_rng(900 + seed)
+        if dim == 2:
+            pts = _points_disk(rng, N)
+            volume = phi * np.pi / N
+            radius = np.sqrt(volume / np.pi)
+        else:
+            pts = rng.random((N, 3)) - 0.5
+            volume = phi / N
+            radius = np.cbrt(3 * volume / (4 * np.pi))
+        alpha = complex(utils.alpha_small_dielectric_object(n_ref, volume))
+        deltas_grid = np.linspace(-3.0, 3.0, 13)
+        solver = cls(torch.from_numpy(pts), source="plane")
+        res = {"points": pts, "k0": k0, "alpha": alpha, "radius": radius, "deltas_grid": deltas_grid}
+        with tempfile.TemporaryDirectory() as tmp, contextlib.redirect_stdout(io.StringIO()):
+            base = os.path.join(tmp, "spec")
+            dos = solver.compute_hamiltonian_DOS(k0, torch.from_numpy(deltas_grid), base)
+            res["hamiltonian_dos"] = dos.numpy()
+            res["ldos_factor"] = float(solver.compute_eigenvalues_and_scatterer_LDOS(k0, alpha, radius, base))
+            res["ldos_factor_no_self"] = float(solver.compute_eigenvalues_and_scatterer_LDOS(
+                k0, alpha, radius, base + "_ns", self_interaction=False, write_eigenvalues=False))
+            for sorting in ("IPR", "damping"):
+                vals, vecs, iprs = solver.compute_eigenmodes_IPR(k0, alpha, radius, base + "_" + sorting,
+                                                                 number_eigenmodes=3, sorting_type=sorting)
+                res[f"ipr_{sorting}_values"] = vals.numpy()
+                res[f"ipr_{sorting}_vectors"] = vecs.numpy()
+                res[f"ipr_{sorting}_iprs"] = iprs.numpy()
+            # the files written, by name relative to the base
+            for name in sorted(os.listdir(tmp)):
+                key = "csv:" + name[len("spec"):]
+                res[key] = np.loadtxt(os.path.join(tmp, name))
+        path = os.path.join(out_dir, f"golden_spectral_{kind}.npz")
+        np.savez_compressed(path, **res)
+        print("wrote", path, os.path.getsize(path), "bytes", sorted(k for k in res if k.startswith("csv:")))
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else os.environ.get("MAGREETE_REFERENCE", "reference")
     if "--greens" in sys.argv:
         main_greens(ref)
+    elif "--spectral" in sys.argv:
+        main_spectral(ref)
     else:
         main(ref)

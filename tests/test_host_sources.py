@@ -190,6 +190,14 @@ def test_class_attributes_and_options(kind, monkeypatch):
     assert cls(pts).precision == "mixed"
     with pytest.raises(ValueError):
         cls(pts, precision="fp16")
-    for name in ("compute_hamiltonian_DOS", "compute_eigenvalues_and_scatterer_LDOS", "compute_eigenmodes_IPR"):
-        with pytest.raises(NotImplementedError):
-            getattr(s, name)()
+    # the spectral tools take the reference's parameters (Transmission2D.py:455, :479, :517)
+    import inspect
+    params = {name: list(inspect.signature(getattr(s, name)).parameters)
+              for name in ("compute_hamiltonian_DOS", "compute_eigenvalues_and_scatterer_LDOS",
+                           "compute_eigenmodes_IPR")}
+    assert params["compute_hamiltonian_DOS"] == ["k0", "deltas", "file_name", "write_eigenvalues"]
+    assert params["compute_eigenvalues_and_scatterer_LDOS"] == [
+        "k0", "alpha", "radius", "file_name", "self_interaction", "self_interaction_type", "write_eigenvalues"]
+    assert params["compute_eigenmodes_IPR"] == [
+        "k0", "alpha", "radius", "file_name", "self_interaction", "self_interaction_type", "number_eigenmodes",
+        "write_eigenvalues", "sorting_type"]
